@@ -1,0 +1,410 @@
+#!/usr/bin/env python
+"""Throughput of the equiprop path on one GB300 (or N replicas).
+
+Workload: d=64, K=4 controls, 65536 steps, Magnus terms with Simpson
+quadrature (131073 samples per control), ||H0|| = 10, ||H_k|| = 1, dt = 1e-3,
+seeded synthetic Hamiltonians and sinusoid-plus-noise controls.  A "step" of
+this benchmark is one full equiprop over the 65536 time steps; the metric is
+time steps per second.
+
+Forms measured:
+  plain_c128 : the reference scheme in complex128 (FP64 arithmetic)
+  plain_c64  : the reference scheme in complex64
+  split_c64  : the split-precision complex64 form (double-float low-order
+               terms, FP64 tree top), when the library provides it
+The headline form is the fastest form whose relative Frobenius error against
+the FP64 result is <= 1e-6.
+
+--impl reference times the reference algorithm's CPU restatement (the C
+oracle, all host threads) on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "equiprop time steps/s (d=64 K=4 Magnus+Simpson, 65536 steps) at <=1e-6 rel err vs FP64"
+UNIT = "steps/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--steps-per-prop", type=int, default=65536, help="time steps of the workload")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_init(n):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def library_gemm_peaks(torch):
+    """cuBLAS FP64 and FP32 (no TF32) GEMM rates, 8192^3, best of 3: the pipe
+    ceilings for the plain complex128 and complex64 forms."""
+    out = {}
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt in (("fp64_gemm_tflops", torch.float64), ("fp32_gemm_tflops", torch.float32)):
+        n = 8192
+        a = torch.randn(n, n, dtype=dt, device="cuda")
+        b = torch.randn(n, n, dtype=dt, device="cuda")
+        best = 0.0
+        for _ in range(3):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.matmul(a, b)
+            e.record()
+            e.synchronize()
+            best = max(best, 2 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+        out[name] = round(best, 2)
+        del a, b
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    return out
+
+
+def flops_per_step(d, M, Ke, form):
+    """Algorithmic flops of one time step: M complex d^3 products (M-1 Clenshaw
+    products after the scalar first term, plus the running product), the
+    assembly (Ke complex multiply-adds per element).  The split form evaluates
+    the same polynomial with its own product count."""
+    gemm = 8.0 * d ** 3
+    if form == "split_c64":
+        return gemm * split_products(M) + 8.0 * Ke * d * d
+    return gemm * M + 8.0 * Ke * d * d
+
+
+def split_products(M):
+    # Y = A^2, then powers Y^2..Y^((M-1)/2) as needed, one odd-part product and
+    # the running product.
+    q = (M - 1) // 2
+    return 1 + max(0, q - 1) + 1 + 1
+
+
+def run_form(torch, parament, w, form, K, W, flush, stream):
+    precision = "fp64" if form == "plain_c128" else "fp32"
+    ctx = parament.Parament(precision)
+    ctx.set_hamiltonian(w["H0"], *w["H1"], use_magnus=True, quadrature_mode="simpson")
+    if form == "split_c64":
+        ctx.set_precision_mode("split")
+    ct = torch.complex128 if precision == "fp64" else torch.complex64
+    carr = torch.tensor(w["carr"], dtype=ct, device="cuda")
+    out = torch.empty((64, 64), dtype=ct, device="cuda")
+    sfx = "_fp64" if precision == "fp64" else ""
+    lib = parament.paramentlib.lib
+    getattr(lib, "Parament_setKernelTiming" + sfx)(ctx._handle, 1)
+    with torch.cuda.stream(stream):
+        for _ in range(W):
+            flush.zero_()
+            ctx.equiprop_device(w["dt"], carr, out, stream)
+        stream.synchronize()
+        evs = []
+        kms = []
+        for _ in range(K):
+            flush.zero_()  # L2 flush between timed steps, outside the events
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            ctx.equiprop_device(w["dt"], carr, out, stream)
+            e.record(stream)
+            evs.append((s, e))
+            kms.append(float(getattr(lib, "Parament_lastKernelMs" + sfx)(ctx._handle)))
+        stream.synchronize()
+    times = [s.elapsed_time(e) for s, e in evs]
+    U = out.cpu().numpy().astype(np.complex128)
+    M = ctx.last_iteration_cycles
+    launches = int(getattr(lib, "Parament_lastLaunchCount" + sfx)(ctx._handle))
+    # End to end through the reference-facing C-ABI with host buffers.
+    e2e = []
+    host_carr = [np.ascontiguousarray(r) for r in w["carr"]]
+    for _ in range(max(2, K)):
+        t0 = time.perf_counter()
+        ctx.equiprop(w["dt"], *host_carr)
+        e2e.append(time.perf_counter() - t0)
+    ctx.destroy()
+    es = 16 if precision == "fp64" else 8
+    return {"ms": times, "kernel_ms": kms, "U": U, "M": M, "launches": launches, "e2e_s": e2e,
+            "h2d": w["carr"].size * es, "d2h": 64 * 64 * es}
+
+
+def cpu_baseline(w, target_s=10.0):
+    """The C restatement of the reference algorithm (oracle) on all host
+    threads, over a bounded prefix of the workload's steps."""
+    import oracle
+    threads = os.cpu_count() or 1
+    hn = oracle.onenorm(w["H0"]) + sum(oracle.onenorm(h) for h in w["H1"])
+    h = 2 * w["dt"]
+    M = oracle.select_cycles(hn, h, fp64=True)
+
+    def sample(S):
+        t0 = time.perf_counter()
+        U = oracle.step_exponentials(w["H0"], w["H1"], w["carr"], w["dt"], True, oracle.SIMPSON, M, hn, 0, S,
+                                     threads)
+        oracle.tree_product(U, threads)
+        return time.perf_counter() - t0
+
+    probe = 4 * threads
+    t = sample(probe)
+    S = int(min(w["P"], max(probe, probe * target_s / max(t, 1e-6))))
+    t = sample(S)
+    return {"value": round(S / t, 2), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {S} of {w['P']} steps (C oracle: Clenshaw exponentials + tree product, FP64), "
+                      f"M={M}"}, S, t
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from parament_gb300 import workloads
+    w = workloads.magnus_d64(args.steps_per_prop)
+    base, S, _ = cpu_baseline(w, target_s=8.0)
+    import oracle
+    threads = os.cpu_count() or 1
+    hn = oracle.onenorm(w["H0"]) + sum(oracle.onenorm(h) for h in w["H1"])
+    M = oracle.select_cycles(hn, 2 * w["dt"], fp64=True)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        U = oracle.step_exponentials(w["H0"], w["H1"], w["carr"], w["dt"], True, oracle.SIMPSON, M, hn, 0, S,
+                                     threads)
+        oracle.tree_product(U, threads)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    v = S * len(times) / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 2), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded; shapes of the d=64 Magnus workload)",
+            "config": {"workload": "magnus_d64_K4_simpson_65536steps", "d": 64, "K": 4, "steps": w["P"],
+                       "samples_per_control": int(w["carr"].shape[1]), "dt": w["dt"],
+                       "sample_steps_per_bench_step": S},
+            "cpu_baseline": {"value": round(v, 2), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"first {S} of {w['P']} steps per bench step (C oracle, FP64)"},
+            "e2e": {"value": round(v, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    import parament_gb300 as parament
+    from parament_gb300 import workloads
+
+    w = workloads.magnus_d64(args.steps_per_prop)
+    P = w["P"]
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    forms = ["plain_c128", "plain_c64", "split_c64"]
+    res = {}
+    for f in forms:
+        try:
+            res[f] = run_form(torch, parament, w, f, args.steps, args.warmup, flush, stream)
+        except (ValueError, RuntimeError) as e:
+            res[f] = {"error": str(e)}
+    ref = res["plain_c128"]["U"]
+    summary = {}
+    for f, r in res.items():
+        if "error" in r:
+            summary[f] = {"error": r["error"]}
+            continue
+        ms = sum(r["ms"]) / len(r["ms"])
+        summary[f] = {"steps_per_s": round(P / (ms * 1e-3), 1), "ms_per_prop": round(ms, 4),
+                      "rel_err_vs_fp64": float(np.linalg.norm(r["U"] - ref) / np.linalg.norm(ref)),
+                      "M": r["M"], "kernel_ms": round(sum(r["kernel_ms"]) / len(r["kernel_ms"]), 4)}
+    ok = [f for f in forms if f in summary and "steps_per_s" in summary[f] and
+          summary[f]["rel_err_vs_fp64"] <= 1e-6]
+    head = max(ok, key=lambda f: summary[f]["steps_per_s"])
+    r = res[head]
+
+    # Timed region for the headline form: K steps bracketed by barrier + sync.
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_dev = []
+        precision = "fp64" if head == "plain_c128" else "fp32"
+        ctx = parament.Parament(precision)
+        ctx.set_hamiltonian(w["H0"], *w["H1"], use_magnus=True, quadrature_mode="simpson")
+        if head == "split_c64":
+            ctx.set_precision_mode("split")
+        ct = torch.complex128 if precision == "fp64" else torch.complex64
+        carr = torch.tensor(w["carr"], dtype=ct, device="cuda")
+        out = torch.empty((64, 64), dtype=ct, device="cuda")
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                ctx.equiprop_device(w["dt"], carr, out, stream)
+            stream.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            evs = []
+            for _ in range(args.steps):
+                flush.zero_()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                ctx.equiprop_device(w["dt"], carr, out, stream)
+                e.record(stream)
+                evs.append((s, e))
+            stream.synchronize()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t_dev = [s.elapsed_time(e) for s, e in evs]
+        ctx.destroy()
+    total_ms = sum(t_dev)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per = total_ms / args.steps
+    value = world * P / (ms_per * 1e-3)
+    if rank != 0:
+        return
+
+    peaks, peak_src = measured_peaks()
+    lib_peaks = library_gemm_peaks(torch)
+    d, K = 64, 4
+    Ke = 2 * K + K * (K - 1) // 2
+    M = r["M"]
+    kms = sum(r["kernel_ms"]) / len(r["kernel_ms"])
+    fl = flops_per_step(d, M, Ke, head) * P
+    achieved = fl / (kms * 1e-3) / 1e12
+    pipe_peak = lib_peaks["fp64_gemm_tflops"] if head == "plain_c128" else lib_peaks["fp32_gemm_tflops"]
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(head)
+    e2e_s = sum(r["e2e_s"]) / len(r["e2e_s"])
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"plain_c128": "c128 (f64)", "plain_c64": "c64 (f32)",
+                  "split_c64": "c64 (f32 + double-float low orders, f64 tree top)"}[head],
+        "data": "synthetic (seeded Hermitian H0/H_k, sinusoid+noise controls)",
+        "config": {"workload": "magnus_d64_K4_simpson_65536steps", "d": d, "K": K, "steps": P,
+                   "samples_per_control": int(w["carr"].shape[1]), "dt": w["dt"], "norm_H0": 10.0,
+                   "form": head, "chebyshev_order": M, "l2": "flushed (512 MiB write) between timed steps",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "forms": summary,
+        "e2e": {"value": round(P / e2e_s, 1), "unit": UNIT, "h2d_bytes_per_step": int(r["h2d"]),
+                "d2h_bytes_per_step": int(r["d2h"]), "api": "Parament_equiprop (host buffers, synchronous)"},
+        "gpu_launches": int(r["launches"]) * args.steps,
+        "roofline": {"bound": "tensor", "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"],
+                     "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 5), "traffic": traffic,
+                     "peak_source": f"{peak_src} bf16 dense (MEASURED_PEAKS.json)",
+                     "kernel": "k_small_steps" if head != "split_c64" else "k_split_steps",
+                     "algorithmic_flops_per_launch": fl, "kernel_ms": round(kms, 4),
+                     "pipe": "fp64" if head == "plain_c128" else "fp32",
+                     "pipe_peak_tflops": pipe_peak, "pipe_frac": round(achieved / pipe_peak, 4),
+                     "pipe_peak_source": "cuBLAS GEMM 8192^3 measured in this run", **lib_peaks},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        base, S, t = cpu_baseline(w)
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, rank, world)
+        return
+    rank, world, local = dist_init(args.gpus)
+    run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

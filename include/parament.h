@@ -1,0 +1,172 @@
+/*
+ * parament-gb300: C-ABI of the GB300-native equiprop library (libparament.so).
+ *
+ * The first block of declarations is the reference library's public interface,
+ * kept name-for-name and type-for-type so that existing callers (the pyparament
+ * ctypes wrapper, C programs) link and run unchanged.  Each declaration cites
+ * the reference declaration it replaces (src/cuda/parament.h, src/cuda/mathhelper.h,
+ * src/cuda/deviceInfo.c inside the parament project).
+ *
+ * The second block adds entry points that the reference does not have
+ * (device-resident inputs, the split-precision form, the adjoint gradient and
+ * batched ensembles).  They take plain pointers and sizes only.
+ *
+ * All matrices are row-major (C order) arrays of interleaved complex numbers.
+ */
+#ifndef PARAMENT_GB300_H_
+#define PARAMENT_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#else
+#include <stdbool.h>
+#endif
+
+#if defined(__GNUC__)
+#define PARAMENT_API __attribute__((visibility("default")))
+#else
+#define PARAMENT_API
+#endif
+
+#ifndef PARAMENT_NO_CUDA_TYPES
+/* Opaque stand-ins for CUDA's complex types when cuComplex.h is not included:
+ * two floats (cuComplex) or two doubles (cuDoubleComplex), real part first. */
+typedef struct cuComplex cuComplex;
+typedef struct cuDoubleComplex cuDoubleComplex;
+#endif
+
+typedef struct Parament_Context_f32 Parament_Context_f32;
+typedef struct Parament_Context_f64 Parament_Context_f64;
+
+/* Quadrature rule; same values as src/cuda/parament.h:64-69. */
+typedef enum Parament_QuadratureSpec {
+    PARAMENT_QUADRATURE_NONE = 0x00000000,
+    PARAMENT_QUADRATURE_MIDPOINT = 0x01000000,
+    PARAMENT_QUADRATURE_SIMPSON = 0x02000000
+} Parament_QuadratureSpec;
+
+/* Error codes; values 0..1000 as src/cuda/parament.h:74-130.  Codes above 1000
+ * are new: they report conditions the reference left undefined. */
+typedef enum Parament_ErrorCode {
+    PARAMENT_STATUS_SUCCESS = 0,
+    PARAMENT_STATUS_HOST_ALLOC_FAILED = 10,
+    PARAMENT_STATUS_DEVICE_ALLOC_FAILED = 20,
+    PARAMENT_STATUS_CUBLAS_INIT_FAILED = 30, /* kept for ABI compatibility; also reported when no CUDA device is usable */
+    PARAMENT_STATUS_INVALID_VALUE = 50,
+    PARAMENT_STATUS_CUBLAS_FAILED = 60, /* kept for ABI compatibility; reported when a kernel launch fails */
+    PARAMENT_STATUS_SELECT_SMALLER_DT = 70,
+    PARAMENT_STATUS_NO_HAMILTONIAN = 80,
+    PARAMENT_STATUS_INVALID_QUADRATURE_SELECTION = 90,
+    PARAMENT_FAIL = 1000,
+    PARAMENT_STATUS_KERNEL_TIMEOUT = 1010 /* a bounded device-side wait gave up (batched queue) */
+} Parament_ErrorCode;
+
+/* ---------------------------------------------------------------- reference ABI */
+
+/* src/cuda/parament.h:155 */
+PARAMENT_API Parament_ErrorCode Parament_create(Parament_Context_f32 **handle_p);
+/* src/cuda/parament.h:177 */
+PARAMENT_API Parament_ErrorCode Parament_destroy(Parament_Context_f32 *handle);
+/* src/cuda/parament.h:219-220.  H1 holds `amps` matrices of dim*dim, back to back. */
+PARAMENT_API Parament_ErrorCode Parament_setHamiltonian(Parament_Context_f32 *handle, cuComplex *H0, cuComplex *H1,
+                                                        unsigned int dim, unsigned int amps, bool use_magnus,
+                                                        Parament_QuadratureSpec quadrature_mode);
+/* src/cuda/parament.h:261-262.  carr holds `amps` arrays of `pts` samples, back to back. */
+PARAMENT_API Parament_ErrorCode Parament_equiprop(Parament_Context_f32 *handle, cuComplex *carr, double dt,
+                                                  unsigned int pts, unsigned int amps, cuComplex *out);
+/* src/cuda/parament.h:286 */
+PARAMENT_API int Parament_selectIterationCycles_fp32(double H_norm, double dt);
+/* src/cuda/parament.h:308 */
+PARAMENT_API Parament_ErrorCode Parament_setIterationCyclesManually(Parament_Context_f32 *handle, unsigned int cycles);
+/* src/cuda/parament.h:327 */
+PARAMENT_API Parament_ErrorCode Parament_automaticIterationCycles(Parament_Context_f32 *handle);
+/* src/cuda/parament.h:347 */
+PARAMENT_API Parament_ErrorCode Parament_peekAtLastError(Parament_Context_f32 *handle);
+/* src/cuda/parament.h:357 */
+PARAMENT_API const char *Parament_errorMessage(Parament_ErrorCode errorCode);
+
+/* src/cuda/parament.h:363 */
+PARAMENT_API Parament_ErrorCode Parament_create_fp64(Parament_Context_f64 **handle_p);
+/* src/cuda/parament.h:368 */
+PARAMENT_API Parament_ErrorCode Parament_destroy_fp64(Parament_Context_f64 *handle);
+/* src/cuda/parament.h:373-374 */
+PARAMENT_API Parament_ErrorCode Parament_setHamiltonian_fp64(Parament_Context_f64 *handle, cuDoubleComplex *H0,
+                                                             cuDoubleComplex *H1, unsigned int dim, unsigned int amps,
+                                                             bool use_magnus, Parament_QuadratureSpec quadrature_mode);
+/* src/cuda/parament.h:379-380 */
+PARAMENT_API Parament_ErrorCode Parament_equiprop_fp64(Parament_Context_f64 *handle, cuDoubleComplex *carr, double dt,
+                                                       unsigned int pts, unsigned int amps, cuDoubleComplex *out);
+/* src/cuda/parament.h:385 */
+PARAMENT_API Parament_ErrorCode Parament_setIterationCyclesManually_fp64(Parament_Context_f64 *handle,
+                                                                         unsigned int cycles);
+/* src/cuda/parament.h:390 */
+PARAMENT_API Parament_ErrorCode Parament_automaticIterationCycles_fp64(Parament_Context_f64 *handle);
+/* src/cuda/parament.h:395 */
+PARAMENT_API Parament_ErrorCode Parament_peekAtLastError_fp64(Parament_Context_f64 *handle);
+/* src/cuda/parament.h:400 */
+PARAMENT_API int Parament_selectIterationCycles_fp64(double H_norm, double dt);
+
+/* src/cuda/mathhelper.h:67 -- maximum absolute row sum of a dim x dim matrix */
+PARAMENT_API double OneNorm(cuComplex *arr, unsigned int dim);
+/* src/cuda/mathhelper.h:68 */
+PARAMENT_API double OneNorm_fp64(cuDoubleComplex *arr, unsigned int dim);
+/* src/cuda/deviceInfo.c:30 -- prints the CUDA devices to stdout */
+PARAMENT_API void device_info(void);
+
+/* ---------------------------------------------------------------- extensions */
+
+/* Precision forms of a context (new; no reference counterpart).
+ *   PARAMENT_PRECISION_PLAIN : the reference scheme in the context's own precision
+ *                              (default; complex128 or complex64 arithmetic).
+ *   PARAMENT_PRECISION_SPLIT : complex64 contexts only.  Step exponentials are
+ *                              formed as U_j = I + E_j with the terms of first and
+ *                              second order in the Hamiltonian in double-float
+ *                              arithmetic and the higher orders in FP32; the
+ *                              running product is accumulated in double-float and
+ *                              the top of the product tree in FP64.  The Chebyshev
+ *                              order is the smallest odd order whose truncation
+ *                              summed over all steps stays below 1e-9. */
+typedef enum Parament_PrecisionMode {
+    PARAMENT_PRECISION_PLAIN = 0,
+    PARAMENT_PRECISION_SPLIT = 1
+} Parament_PrecisionMode;
+
+PARAMENT_API Parament_ErrorCode Parament_setPrecisionMode(Parament_Context_f32 *handle, int mode);
+PARAMENT_API int Parament_getPrecisionMode(Parament_Context_f32 *handle);
+
+/* Chebyshev order used by the last successful equiprop (0 before the first). */
+PARAMENT_API int Parament_lastIterationCycles(Parament_Context_f32 *handle);
+PARAMENT_API int Parament_lastIterationCycles_fp64(Parament_Context_f64 *handle);
+
+/* Norm bound Hnorm = ||H0||_inf + sum_k ||H_k||_inf of the loaded Hamiltonian (0 if none). */
+PARAMENT_API double Parament_hamiltonianNorm(Parament_Context_f32 *handle);
+PARAMENT_API double Parament_hamiltonianNorm_fp64(Parament_Context_f64 *handle);
+
+/* equiprop on device-resident buffers (new; the reference copies from host
+ * memory at src/cuda/parament.cpp:477 and back at :846).  d_carr and d_out are
+ * device pointers; the work is queued on `stream` (a cudaStream_t, or NULL for
+ * the context's own stream) and the call returns without waiting. */
+PARAMENT_API Parament_ErrorCode Parament_equipropDevice(Parament_Context_f32 *handle, const void *d_carr, double dt,
+                                                        unsigned int pts, unsigned int amps, void *d_out,
+                                                        void *stream);
+PARAMENT_API Parament_ErrorCode Parament_equipropDevice_fp64(Parament_Context_f64 *handle, const void *d_carr,
+                                                             double dt, unsigned int pts, unsigned int amps,
+                                                             void *d_out, void *stream);
+
+/* Instrumentation (new).  With timing enabled, each equiprop records CUDA
+ * events on its stream around its dominant kernel (the fused step kernel, or
+ * the step batches of the large-d path); Parament_lastKernelMs waits for the
+ * stop event and returns that duration in milliseconds (-1 when disabled).
+ * Parament_lastLaunchCount returns the number of kernels the last call launched. */
+PARAMENT_API Parament_ErrorCode Parament_setKernelTiming(Parament_Context_f32 *handle, int enable);
+PARAMENT_API Parament_ErrorCode Parament_setKernelTiming_fp64(Parament_Context_f64 *handle, int enable);
+PARAMENT_API float Parament_lastKernelMs(Parament_Context_f32 *handle);
+PARAMENT_API float Parament_lastKernelMs_fp64(Parament_Context_f64 *handle);
+PARAMENT_API int Parament_lastLaunchCount(Parament_Context_f32 *handle);
+PARAMENT_API int Parament_lastLaunchCount_fp64(Parament_Context_f64 *handle);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARAMENT_GB300_H_ */

@@ -1,0 +1,84 @@
+// Context state behind the opaque Parament_Context_f32/_f64 handles.
+//
+// Mirrors what src/cuda/parament_context.hpp:26-78 keeps (dimension, norm
+// bound, order control, quadrature settings, last error) with a new layout:
+// one expansion stack [H0, H_k, commutators] instead of separate H0/H1
+// buffers, grow-only work buffers, and a private non-blocking stream.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "parament.h"
+
+namespace pgb {
+
+bool fault_inject_alloc();
+
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    void release();
+};
+
+struct Ctx {
+    bool fp64 = false;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    Parament_ErrorCode last_error = PARAMENT_STATUS_SUCCESS;
+
+    // Hamiltonian (src/cuda/parament_context.hpp:37-56)
+    bool has_h = false;
+    unsigned dim = 0, K = 0, Ke = 0;
+    bool magnus = true;                          // defaults as src/cuda/parament.cpp:72-75
+    int quad = PARAMENT_QUADRATURE_SIMPSON;
+    double hnorm = 0.0;
+    DevBuf stack;                                // (1+Ke) d x d, context precision
+
+    // Chebyshev order control (src/cuda/parament_context.hpp:72-73)
+    unsigned mmax = 11;
+    bool manual = false;
+    int last_M = 0;
+
+    // Precision form (complex64 contexts)
+    int precision = PARAMENT_PRECISION_PLAIN;
+    DevBuf split_stack;                          // double-float copy of the stack
+    bool split_ready = false;
+
+    // Instrumentation: CUDA events around the dominant kernel of the last call
+    // and the number of kernels it launched.
+    bool timing = false;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    int launches = 0;
+
+    // Work buffers (grow-only, like src/cuda/parament.cpp:418-474)
+    DevBuf carr, out, chunks, work, X, B1, B2, aux;
+
+    size_t esize() const { return fp64 ? 16 : 8; }
+    void release_all() {
+        stack.release();
+        split_stack.release();
+        carr.release();
+        out.release();
+        chunks.release();
+        work.release();
+        X.release();
+        B1.release();
+        B2.release();
+        aux.release();
+    }
+};
+
+double onenorm_host(const void *m, unsigned d, bool fp64);
+int select_cycles(bool fp64, double hnorm, double dt);
+void bessel_coeffs(int M, double x, double *J);
+long long num_steps(int quad, bool magnus, unsigned pts);
+
+// Split-precision form (complex64 contexts): order choice and propagation.
+int split_order(double hnorm, double h, long long P);
+Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned amps, double h, int M, long long P,
+                             void *d_out, cudaStream_t stream);
+
+}  // namespace pgb

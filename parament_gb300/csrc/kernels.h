@@ -1,0 +1,103 @@
+// Host-side launch interface of the equiprop kernels (no CUDA device code here).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace pgb {
+
+// Maximum Chebyshev order accepted by the kernels (the fp64 order table stops at 41).
+constexpr int kMaxOrder = 63;
+
+struct WeightSpecHost {
+    unsigned pts;
+    int K;
+    int amps;
+    int mode;
+    int magnus;
+    double hfac;
+};
+
+// One plain-path propagation over the steps [0, P): the fused small-d kernel
+// (d <= kSmallMaxDim) writes one ordered product per chunk of consecutive
+// steps into `chunks`.
+constexpr int kSmallMaxDim = 64;
+
+struct StepLaunch {
+    bool fp64;
+    int d;
+    int Ke;                   // expansion matrices beside H0
+    WeightSpecHost w;
+    int M;                    // odd Chebyshev order
+    const double *J;          // 2*(M+1) doubles: (-i)^k J_k(x), k=0..M
+    double s;                 // 2 / Hnorm
+    const void *stack;        // (1+Ke) d x d matrices, context precision
+    const void *carr;         // amps x pts samples, context precision
+    void *chunks;             // nchunks d x d products (output)
+    long long P;              // steps
+    int nchunks;
+    cudaStream_t stream;
+};
+
+// Number of chunks the small kernel uses for P steps (one wave of resident CTAs).
+int small_chunk_count(bool fp64, int d, int Ke, long long P, int num_sms);
+size_t small_smem_bytes(bool fp64, int d, int Ke);
+cudaError_t launch_small_steps(const StepLaunch &a);
+
+// C_b = alpha * A_b B_b + beta * Cin_b + diag * I for b < batch (all d x d,
+// row-major; strides in elements).  Cin may alias Cout.  Cin may be null
+// when beta == 0.
+struct GemmLaunch {
+    bool fp64;
+    int d;
+    int batch;
+    const void *A;
+    long long strideA;
+    const void *B;
+    long long strideB;
+    const void *Cin;
+    long long strideCin;
+    void *Cout;
+    long long strideCout;
+    double alpha_re, alpha_im;
+    double beta;
+    double diag_re, diag_im;
+    cudaStream_t stream;
+    int num_sms;
+};
+cudaError_t launch_gemm(const GemmLaunch &g);
+
+// Ordered product of n d x d matrices (later index on the left), pairwise tree
+// as src/cuda/parament.cpp:677-714.  `work` holds n*d*d elements and may be
+// overwritten; `in` is overwritten too.  The result is copied into `out`.
+// *levels (if given) receives the number of kernel launches.
+cudaError_t tree_product(bool fp64, int d, void *in, long long n, void *work, void *out, cudaStream_t stream,
+                         int num_sms, int *levels = nullptr);
+
+// Large-d plain path: the steps [s0, s1) are assembled, exponentiated and
+// multiplied into one product written to `out`.  Buffers: X, B1, B2 each hold
+// `batch` matrices.
+struct LargeLaunch {
+    bool fp64;
+    int d;
+    int Ke;
+    WeightSpecHost w;
+    int M;
+    const double *J;
+    double s;
+    const void *stack;
+    const void *carr;
+    long long s0, s1;
+    int batch;
+    void *X, *B1, *B2;
+    void *out;
+    cudaStream_t stream;
+    int num_sms;
+};
+cudaError_t launch_large_range(const LargeLaunch &a, int *launches = nullptr);
+
+// Device-side copies and fills.
+cudaError_t fill_identity(bool fp64, void *dst, int d, long long count, double scale_re, double scale_im,
+                          cudaStream_t stream);
+
+}  // namespace pgb
