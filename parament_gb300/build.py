@@ -38,13 +38,35 @@ def _headers():
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
+def _lib_matches(arch: str) -> bool:
+    """True when the existing libparament.so is an ELF file for this host."""
+    machine = {"x86_64": 62, "aarch64": 183}.get(arch)
+    try:
+        with open(LIB, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return False
+    return machine is not None and len(head) == 20 and head[:4] == b"\x7fELF" and \
+        int.from_bytes(head[18:20], "little") == machine
+
+
 def _stale(obj: str, src: str, hdr_mtime: float) -> bool:
     return not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_mtime)
 
 
 def build(verbose: bool = False, force: bool = False, extra_flags=None) -> str:
+    import platform
+
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
+    # Objects from another host architecture (a copied tree) are never reused.
+    stamp = os.path.join(BUILD, "host_arch")
+    arch = platform.machine()
+    if not os.path.exists(stamp) or open(stamp).read().strip() != arch or \
+            (os.path.exists(LIB) and not _lib_matches(arch)):
+        force = True
+        with open(stamp, "w") as f:
+            f.write(arch)
     hdr_mtime = max(os.path.getmtime(h) for h in _headers())
     srcs = _sources()
     objs = [os.path.join(BUILD, os.path.basename(s) + ".o") for s in srcs]
