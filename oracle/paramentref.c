@@ -38,6 +38,14 @@
 
 typedef double complex cplx;
 
+/* Rounds the real and imaginary parts to float: the complex64 context keeps
+ * its Bessel coefficients, scale factor and step weights in float
+ * (src/cuda/mathhelper.cpp:19-32, src/cuda/parament.cpp:583-584,
+ * src/cuda/control_expansion.cu:27-60).  Those roundings repeat identically at
+ * every step, so they shift the result coherently; the oracle reproduces them
+ * and keeps everything else in FP64. */
+static cplx round_c64(cplx z) { return (double)(float)creal(z) + I * (double)(float)cimag(z); }
+
 enum { PR_NONE = 0, PR_MIDPOINT = 0x01000000, PR_SIMPSON = 0x02000000 };
 
 /* Order tables: thresholds on Hnorm*dt and the odd orders they select.
@@ -208,7 +216,7 @@ typedef struct {
     const cplx *J;
     cplx *U;
     unsigned d, pts, amps, K, Ke;
-    int mode, magnus, M;
+    int mode, magnus, M, single;
     double h, s;
     long s0, s1;
 } step_job;
@@ -220,7 +228,10 @@ static void *step_worker(void *arg) {
     cplx *X = malloc(sizeof(cplx) * dd);
     cplx *work = malloc(sizeof(cplx) * dd * 3);
     for (long s = jb->s0; s < jb->s1; ++s) {
-        pr_step_weights(jb->carr, jb->pts, jb->amps, jb->K, jb->mode, jb->magnus, jb->h, s, w);
+        pr_step_weights(jb->carr, jb->pts, jb->amps, jb->K, jb->mode, jb->magnus,
+                        jb->single ? (double)(float)jb->h : jb->h, s, w);
+        if (jb->single)
+            for (unsigned m = 0; m < jb->Ke; ++m) w[m] = round_c64(w[m]);
         pr_assemble(jb->stack, jb->d, jb->Ke, w, X);
         pr_clenshaw(X, jb->d, jb->M, jb->J, jb->s, jb->U + s * dd, work);
     }
@@ -276,9 +287,12 @@ static void tree_reduce(cplx *mats, long P, unsigned d, int nthreads) {
     free(tmp);
 }
 
+
 /* Full equiprop restatement (src/cuda/parament.cpp:791-851).
- *   single   : 1 selects the single-precision order table and float moduli in
- *              the norm (the reference's complex64 context), 0 the fp64 ones.
+ *   single   : 1 = the reference's complex64 context: single-precision order
+ *              table, float moduli in the norm, and the float roundings of the
+ *              Bessel coefficients, the scale 2/Hnorm and the step weights;
+ *              0 = the complex128 context.
  *   M_manual : > 0 forces the Chebyshev order (setIterationCyclesManually).
  *   nthreads : host threads for the step exponentials and each tree level.
  * Returns 0 on success, 70 when the order table overflows, 50 when the
@@ -310,13 +324,18 @@ int pr_equiprop(const cplx *H0, const cplx *H1, unsigned d, unsigned K, int magn
     pr_build_stack(H0, H1, d, K, magnus, stack);
     pr_bessel_coeffs(M, h * hnorm, J);
     double s = 2.0 / hnorm;
+    if (single) {
+        for (int k = 0; k <= M; ++k) J[k] = round_c64(J[k]);
+        s = (double)(float)s;
+    }
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     int nt = nthreads < P ? nthreads : (int)P;
     pthread_t th[256];
     step_job jobs[256];
     for (int t = 0; t < nt; ++t) {
-        jobs[t] = (step_job){stack, carr, J, U, d, pts, amps, K, Ke, mode, magnus, M, h, s, P * t / nt, P * (t + 1) / nt};
+        jobs[t] = (step_job){stack, carr, J, U, d, pts, amps, K, Ke, mode, magnus, M, single, h, s, P * t / nt,
+                             P * (t + 1) / nt};
         if (nt > 1)
             pthread_create(&th[t], NULL, step_worker, &jobs[t]);
         else
@@ -356,7 +375,7 @@ int pr_step_exponentials(const cplx *H0, const cplx *H1, unsigned d, unsigned K,
     pthread_t th[256];
     step_job jobs[256];
     for (int t = 0; t < nt; ++t) {
-        jobs[t] = (step_job){stack, carr, J, U - s0 * dd, d, pts, amps, K, Ke, mode, magnus, M, h, 2.0 / hnorm,
+        jobs[t] = (step_job){stack, carr, J, U - s0 * dd, d, pts, amps, K, Ke, mode, magnus, M, 0, h, 2.0 / hnorm,
                              s0 + P * t / nt, s0 + P * (t + 1) / nt};
         if (nt > 1)
             pthread_create(&th[t], NULL, step_worker, &jobs[t]);
