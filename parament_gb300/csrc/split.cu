@@ -1,17 +1,554 @@
-// Split-precision form for complex64 contexts (placeholder until the kernels land).
+// Split-precision form of the equiprop path for complex64 contexts, d <= 64.
+//
+// Why: over tens of thousands of steps, any rounding that repeats identically
+// at every step (the float copies of H0, of 2/Hnorm, of the Bessel
+// coefficients) adds up coherently; in plain complex64 that alone costs ~1e-4
+// relative error.  Here the step exponential is written U_j = I + E_j and the
+// Chebyshev-Bessel polynomial of the reference (the same coefficients
+// (-i)^k J_k(x), src/cuda/mathhelper.cpp:69-80) is regrouped by powers of X_j:
+//
+//   E_j = (m_0 - 1) I + mu_1 X + mu_2 X^2 + X (mu_3 X^2 + mu_5 X^4 + ...) + mu_4 X^4 + ...
+//
+// with mu_n = m_n / Hnorm^n and m_n the monomial coefficients of
+// J_0 + 2 sum_k (-i)^k J_k(x) T_k(t).  The first- and second-order terms
+// (|mu_1 X| ~ Hnorm dt, |mu_2 X^2| ~ (Hnorm dt)^2) are formed in double-float
+// (pairs of floats) from a double-float copy of the expansion stack; X^2 uses
+// the three products hi*hi + hi*lo + lo*hi; the higher orders, whose size is
+// below 1e-5 of the result, stay in FP32.  Each CTA multiplies its chunk of
+// consecutive steps into E^P (P = I + E^P) held in double-float, adding the
+// FP32 product E_j E^P; the chunk products are then combined by the FP64 tree.
+//
+// The Chebyshev order is the smallest odd M >= 3 whose truncation, summed over
+// all P steps (2 P |J_(M+1)(x)|), stays below 1e-9; x = Hnorm * dt_eff must
+// not exceed 0.5 so that the regrouped polynomial has no cancellation.
 #include <math.h>
 
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
 #include "ctx.h"
+#include "kernels.h"
 
 namespace pgb {
 
-int split_order(double hnorm, double h, long long P) {
-    (void)P;
-    return select_cycles(true, hnorm, h);
+constexpr int kSplitMaxOrder = 15;
+constexpr double kSplitMaxX = 0.5;
+
+// ---------------------------------------------------------------- double-float
+
+struct df {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df df_from(double v) {
+    float h = (float)v;
+    return {h, (float)(v - (double)h)};
+}
+// s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ df df_norm(float hi, float lo) {
+    float s = __fadd_rn(hi, lo);
+    return {s, __fsub_rn(lo, __fsub_rn(s, hi))};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return df_norm(s, e);
+}
+__device__ __forceinline__ df df_add_f(df a, float b) {
+    float s, e;
+    two_sum(a.hi, b, s, e);
+    return df_norm(s, __fadd_rn(e, a.lo));
+}
+// a * b to about 2^-44 relative (the lo*lo term is dropped).
+__device__ __forceinline__ df df_mul(df a, df b) {
+    float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return df_norm(p, e);
+}
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+    float p = __fmul_rn(a.hi, b);
+    float e = __fmaf_rn(a.hi, b, -p);
+    e = __fmaf_rn(a.lo, b, e);
+    return df_norm(p, e);
+}
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+
+struct cdf {
+    df re, im;
+};
+__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
+__device__ __forceinline__ cdf cdf_add_c(cdf a, float2 b) { return {df_add_f(a.re, b.x), df_add_f(a.im, b.y)}; }
+__device__ __forceinline__ cdf cdf_mul(cdf a, cdf b) {
+    return {df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im))), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+// a * b with b a float complex.
+__device__ __forceinline__ cdf cdf_mul_c(cdf a, float2 b) {
+    return {df_add(df_mul_f(a.re, b.x), df_neg(df_mul_f(a.im, b.y))), df_add(df_mul_f(a.re, b.y), df_mul_f(a.im, b.x))};
+}
+__device__ __forceinline__ float2 cdf_hi(cdf a) { return make_float2(a.re.hi, a.im.hi); }
+__device__ __forceinline__ float2 cdf_lo(cdf a) { return make_float2(a.re.lo, a.im.lo); }
+
+// ---------------------------------------------------------------- kernel
+
+struct SplitArgs {
+    double2 c0;                         // m_0 - 1
+    double2 mu[kSplitMaxOrder + 1];     // mu_n, n = 1..M
+    const float4 *stack;                // (1+Ke) matrices: (re_hi, im_hi, re_lo, im_lo)
+    const float2 *carr;                 // samples (complex64)
+    double2 *chunks;                    // nchunks products I + E^P, complex128
+    long long P;
+    int nchunks;
+    int d, Ke, M;
+    unsigned pts;
+    int K, amps, mode, magnus;
+    double hfac;
+};
+
+// Weight m of step s in FP64 from complex64 samples (src/cuda/control_expansion.cu:27-170,
+// pair slots re-indexed as in step_weight).
+__device__ double2 split_weight(const SplitArgs &a, int m, long long s) {
+    const size_t pts = a.pts;
+    auto ld = [&](int k, long long i) {
+        float2 v = a.carr[(size_t)k * pts + i];
+        return make_double2(v.x, v.y);
+    };
+    if (m < a.K) {
+        if (m >= a.amps) return make_double2(0, 0);
+        if (a.magnus || a.mode == kQuadSimpson) {
+            double2 x = ld(m, 2 * s), y = ld(m, 2 * s + 1), z = ld(m, 2 * s + 2);
+            return make_double2((x.x + 4.0 * y.x + z.x) / 6.0, (x.y + 4.0 * y.y + z.y) / 6.0);
+        }
+        if (a.mode == kQuadMidpoint) {
+            double2 x = ld(m, s), y = ld(m, s + 1);
+            return make_double2(0.5 * (x.x + y.x), 0.5 * (x.y + y.y));
+        }
+        return ld(m, s);
+    }
+    const double2 f = make_double2(0.0, a.hfac);
+    if (m < 2 * a.K) {
+        int k = m - a.K;
+        if (k >= a.amps) return make_double2(0, 0);
+        return cmul(csub(ld(k, 2 * s + 2), ld(k, 2 * s)), f);
+    }
+    int p = m - 2 * a.K;
+    int i = 1;
+    while ((i + 1) * i / 2 <= p) ++i;
+    int j = p - i * (i - 1) / 2;
+    if (i >= a.amps) return make_double2(0, 0);
+    double2 t = csub(cmul(ld(j, 2 * s), ld(i, 2 * s + 2)), cmul(ld(j, 2 * s + 2), ld(i, 2 * s)));
+    return cmul(t, f);
 }
 
-Parament_ErrorCode run_split(Ctx *, const void *, unsigned, unsigned, double, int, long long, void *, cudaStream_t) {
-    return PARAMENT_STATUS_INVALID_VALUE;
+// acc = A * B (+ A2 * B2 when TWO) over the thread's micro-tile.
+template <int TM, bool TWO>
+__device__ __forceinline__ void tile_gemm_f(float2 (&acc)[TM][TM], const float2 *__restrict__ A,
+                                            const float2 *__restrict__ B, const float2 *__restrict__ A2,
+                                            const float2 *__restrict__ B2, int d, int ty, int tx) {
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TM; ++j) acc[i][j] = make_float2(0.f, 0.f);
+    int ro[TM], co[TM];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        ro[i] = min(ty + 16 * i, d - 1) * d;
+        co[i] = min(tx + 16 * i, d - 1);
+    }
+#pragma unroll 4
+    for (int k = 0; k < d; ++k) {
+        float2 av[TM], bv[TM];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) av[i] = A[ro[i] + k];
+#pragma unroll
+        for (int j = 0; j < TM; ++j) bv[j] = B[k * d + co[j]];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j) cfma(acc[i][j], av[i], bv[j]);
+        if (TWO) {
+#pragma unroll
+            for (int i = 0; i < TM; ++i) av[i] = A2[ro[i] + k];
+#pragma unroll
+            for (int j = 0; j < TM; ++j) bv[j] = B2[k * d + co[j]];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) cfma(acc[i][j], av[i], bv[j]);
+        }
+    }
+}
+
+__device__ __forceinline__ float2 cmulf_d(double2 mu, float2 g) {
+    // float product of a FP64 coefficient (rounded) and a float value.
+    return cmul(make_float2((float)mu.x, (float)mu.y), g);
+}
+
+template <int TM>
+__global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ SplitArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int d = a.d, dd = d * d;
+    float2 *Xh = reinterpret_cast<float2 *>(smem_raw);  // X hi
+    float2 *Xl = Xh + dd;                               // X lo, later Q (odd part)
+    float2 *G2 = Xl + dd;                               // X^2, later E hi
+    float2 *Gc = G2 + dd;                               // X^(2k)
+    float2 *Ph = Gc + dd;                               // E^P hi
+    float2 *Pl = Ph + dd;                               // E^P lo
+    double2 *ws = reinterpret_cast<double2 *>(Pl + dd); // step weights
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const long long s0 = a.P * blockIdx.x / a.nchunks;
+    const long long s1 = a.P * (blockIdx.x + 1) / a.nchunks;
+    const int M = a.M;
+
+    int eo[TM][TM];
+    bool own[TM][TM], dg[TM][TM];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TM; ++j) {
+            int r = ty + 16 * i, c = tx + 16 * j;
+            own[i][j] = r < d && c < d;
+            eo[i][j] = r * d + c;
+            dg[i][j] = r == c;
+        }
+    const cdf mu1 = {df_from(a.mu[1].x), df_from(a.mu[1].y)};
+    const cdf mu2 = {df_from(a.mu[2].x), df_from(a.mu[2].y)};
+    const cdf c0 = {df_from(a.c0.x), df_from(a.c0.y)};
+
+    cdf E[TM][TM];
+    float2 acc[TM][TM], Q[TM][TM];
+    for (long long st = s0; st < s1; ++st) {
+        for (int m = tid; m < a.Ke; m += blockDim.x) ws[m] = split_weight(a, m, st);
+        __syncthreads();
+        // X = H0 + sum_m w_m H_m in double-float; E starts as (m_0-1) I + mu_1 X.
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j) {
+                if (!own[i][j]) continue;
+                const int e = eo[i][j];
+                float4 h = a.stack[e];
+                cdf x = {{h.x, h.z}, {h.y, h.w}};
+                for (int m = 0; m < a.Ke; ++m) {
+                    float4 g = a.stack[(size_t)(m + 1) * dd + e];
+                    double2 w = ws[m];
+                    cdf wd = {df_from(w.x), df_from(w.y)};
+                    x = cdf_add(x, cdf_mul(wd, cdf{{g.x, g.z}, {g.y, g.w}}));
+                }
+                Xh[e] = cdf_hi(x);
+                Xl[e] = cdf_lo(x);
+                cdf v = cdf_mul(mu1, x);
+                if (dg[i][j]) v = cdf_add(v, c0);
+                E[i][j] = v;
+            }
+        __syncthreads();
+        // G2 = X^2 = Xh Xh + (Xh Xl + Xl Xh).
+        tile_gemm_f<TM, false>(acc, Xh, Xh, nullptr, nullptr, d, ty, tx);
+        {
+            float2 cr[TM][TM];
+            tile_gemm_f<TM, true>(cr, Xh, Xl, Xl, Xh, d, ty, tx);
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) acc[i][j] = make_float2(acc[i][j].x + cr[i][j].x, acc[i][j].y + cr[i][j].y);
+        }
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j) {
+                if (!own[i][j]) continue;
+                E[i][j] = cdf_add(E[i][j], cdf_mul_c(mu2, acc[i][j]));
+                Q[i][j] = (M >= 3) ? cmulf_d(a.mu[3], acc[i][j]) : make_float2(0.f, 0.f);
+                G2[eo[i][j]] = acc[i][j];
+                Gc[eo[i][j]] = acc[i][j];
+            }
+        __syncthreads();
+        // Higher even powers X^(2k) = X^(2k-2) X^2 in FP32.
+        for (int k = 2; 2 * k <= M; ++k) {
+            tile_gemm_f<TM, false>(acc, Gc, G2, nullptr, nullptr, d, ty, tx);
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) {
+                    if (!own[i][j]) continue;
+                    E[i][j] = cdf_add_c(E[i][j], cmulf_d(a.mu[2 * k], acc[i][j]));
+                    if (2 * k + 1 <= M) {
+                        float2 q = cmulf_d(a.mu[2 * k + 1], acc[i][j]);
+                        Q[i][j] = make_float2(Q[i][j].x + q.x, Q[i][j].y + q.y);
+                    }
+                    Gc[eo[i][j]] = acc[i][j];
+                }
+            __syncthreads();
+        }
+        // Odd part X * Q.
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j)
+                if (own[i][j]) Xl[eo[i][j]] = Q[i][j];
+        __syncthreads();
+        tile_gemm_f<TM, false>(acc, Xh, Xl, nullptr, nullptr, d, ty, tx);
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j) {
+                if (!own[i][j]) continue;
+                E[i][j] = cdf_add_c(E[i][j], acc[i][j]);
+            }
+        // Running product: E^P <- E^P + E + E E^P.
+        if (st == s0) {
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) {
+                        Ph[eo[i][j]] = cdf_hi(E[i][j]);
+                        Pl[eo[i][j]] = cdf_lo(E[i][j]);
+                    }
+            __syncthreads();
+        } else {
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) G2[eo[i][j]] = cdf_hi(E[i][j]);
+            __syncthreads();
+            tile_gemm_f<TM, false>(acc, G2, Ph, nullptr, nullptr, d, ty, tx);
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) {
+                    if (!own[i][j]) continue;
+                    const int e = eo[i][j];
+                    float2 ph = Ph[e], pl = Pl[e];
+                    cdf p = {{ph.x, pl.x}, {ph.y, pl.y}};
+                    p = cdf_add(p, E[i][j]);
+                    p = cdf_add_c(p, acc[i][j]);
+                    Ph[e] = cdf_hi(p);
+                    Pl[e] = cdf_lo(p);
+                }
+            __syncthreads();
+        }
+    }
+    if (s1 > s0) {
+        double2 *dst = a.chunks + (size_t)blockIdx.x * dd;
+        for (int e = tid; e < dd; e += blockDim.x) {
+            float2 ph = Ph[e], pl = Pl[e];
+            double re = (double)ph.x + (double)pl.x, im = (double)ph.y + (double)pl.y;
+            if (e / d == e % d) re += 1.0;
+            dst[e] = make_double2(re, im);
+        }
+    }
+}
+
+__global__ void k_c128_to_c64(const double2 *src, float2 *dst, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = make_float2((float)src[i].x, (float)src[i].y);
+}
+
+// Double-float stack from the FP64 stack: (re_hi, im_hi, re_lo, im_lo).
+__global__ void k_split_stack(const double2 *src, float4 *dst, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double2 v = src[i];
+        float rh = (float)v.x, ih = (float)v.y;
+        dst[i] = make_float4(rh, ih, (float)(v.x - (double)rh), (float)(v.y - (double)ih));
+    }
+}
+__global__ void k_c64_to_c128(const float2 *src, double2 *dst, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = make_double2(src[i].x, src[i].y);
+}
+
+static size_t split_smem(int d, int Ke) { return 6 * (size_t)d * d * sizeof(float2) + (size_t)std::max(Ke, 1) * 16; }
+
+template <int TM>
+static const void *split_kernel_ptr() {
+    return reinterpret_cast<const void *>(&k_split_steps<TM>);
+}
+static const void *pick_split(int d) {
+    switch ((d + 15) / 16) {
+        case 1: return split_kernel_ptr<1>();
+        case 2: return split_kernel_ptr<2>();
+        case 3: return split_kernel_ptr<3>();
+        default: return split_kernel_ptr<4>();
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+int split_order(double hnorm, double h, long long P) {
+    const double x = hnorm * h;
+    if (!(x <= kSplitMaxX)) return -1;
+    for (int M = 3; M <= kSplitMaxOrder; M += 2)
+        if (2.0 * (double)P * fabs(jn(M + 1, x)) <= 1e-9) return M;
+    return kSplitMaxOrder;
+}
+
+// Monomial coefficients m_n of J_0(x) + 2 sum_(k=1..M) (-i)^k J_k(x) T_k(t);
+// returns mu_n = m_n / Hnorm^n (n >= 1) and c0 = m_0 - 1.
+static void split_coefficients(int M, double x, double hnorm, double *c0, std::vector<double> &mu) {
+    std::vector<double> J(2 * (M + 1));
+    bessel_coeffs(M, x, J.data());
+    std::vector<double> re(M + 1, 0.0), im(M + 1, 0.0);
+    std::vector<double> tkm1(M + 1, 0.0), tk(M + 1, 0.0), tkp1(M + 1, 0.0);
+    tkm1[0] = 1.0;  // T_0
+    if (M >= 1) tk[1] = 1.0;  // T_1
+    // m_0 - 1 computed without forming 1 + small - 1.
+    double c0r = jn(0, x) - 1.0, c0i = 0.0;
+    for (int k = 1; k <= M; ++k) {
+        for (int n = 0; n <= M; ++n) {
+            double t = 2.0 * tk[n];  // tk holds the monomial coefficients of T_k
+            if (t == 0.0) continue;
+            if (n == 0) {
+                c0r += t * J[2 * k];
+                c0i += t * J[2 * k + 1];
+            } else {
+                re[n] += t * J[2 * k];
+                im[n] += t * J[2 * k + 1];
+            }
+        }
+        // T_(k+1) = 2 t T_k - T_(k-1)
+        for (int n = 0; n <= M; ++n) tkp1[n] = (n > 0 ? 2.0 * tk[n - 1] : 0.0) - tkm1[n];
+        tkm1 = tk;
+        tk = tkp1;
+    }
+    c0[0] = c0r;
+    c0[1] = c0i;
+    mu.assign(2 * (M + 1), 0.0);
+    double scale = 1.0;
+    for (int n = 1; n <= M; ++n) {
+        scale /= hnorm;
+        mu[2 * n] = re[n] * scale;
+        mu[2 * n + 1] = im[n] * scale;
+    }
+}
+
+// Builds the double-float stack: the complex64 inputs promoted to FP64, the
+// Magnus commutators recomputed in FP64, split into float pairs.
+static Parament_ErrorCode prepare_split_stack(Ctx *c) {
+    if (c->split_ready) return PARAMENT_STATUS_SUCCESS;
+    const size_t dd = (size_t)c->dim * c->dim, n = dd * (1 + c->Ke);
+    DevBuf tmp;
+    if (tmp.ensure(n * sizeof(double2)) != cudaSuccess || c->split_stack.ensure(n * sizeof(float4)) != cudaSuccess) {
+        tmp.release();
+        return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+    }
+    double2 *s64 = static_cast<double2 *>(tmp.ptr);
+    const float2 *s32 = static_cast<const float2 *>(c->stack.ptr);
+    const unsigned K = c->K;
+    const size_t base = c->magnus ? dd * (1 + K) : n;  // inputs: H0 and H_1..H_K
+    k_c64_to_c128<<<256, 256, 0, c->stream>>>(s32, s64, (long long)base);
+    cudaError_t e = cudaGetLastError();
+    auto commutator = [&](size_t x, size_t y, size_t dst) -> cudaError_t {
+        GemmLaunch g{};
+        g.fp64 = true;
+        g.d = (int)c->dim;
+        g.batch = 1;
+        g.A = s64 + dd * x;
+        g.B = s64 + dd * y;
+        g.Cout = s64 + dd * dst;
+        g.alpha_re = 1.0;
+        g.stream = c->stream;
+        g.num_sms = c->num_sms;
+        cudaError_t r = launch_gemm(g);
+        if (r != cudaSuccess) return r;
+        g.A = s64 + dd * y;
+        g.B = s64 + dd * x;
+        g.Cin = s64 + dd * dst;
+        g.alpha_re = -1.0;
+        g.beta = 1.0;
+        return launch_gemm(g);
+    };
+    if (c->magnus) {
+        for (unsigned k = 0; k < K && e == cudaSuccess; ++k) e = commutator(0, 1 + k, 1 + K + k);
+        for (unsigned i = 1; i < K && e == cudaSuccess; ++i)
+            for (unsigned j = 0; j < i && e == cudaSuccess; ++j)
+                e = commutator(1 + j, 1 + i, 1 + 2 * K + i * (i - 1) / 2 + j);
+    }
+    if (e == cudaSuccess) {
+        k_split_stack<<<512, 256, 0, c->stream>>>(s64, static_cast<float4 *>(c->split_stack.ptr), (long long)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    tmp.release();
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return PARAMENT_STATUS_CUBLAS_FAILED;
+    }
+    c->split_ready = true;
+    return PARAMENT_STATUS_SUCCESS;
+}
+
+Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned amps, double h, int M, long long P,
+                             void *d_out, cudaStream_t stream) {
+    const int d = (int)c->dim;
+    if (d > kSmallMaxDim) return PARAMENT_STATUS_INVALID_VALUE;
+    if (M > kSplitMaxOrder || c->hnorm * h > kSplitMaxX) return PARAMENT_STATUS_SELECT_SMALLER_DT;
+    Parament_ErrorCode r = prepare_split_stack(c);
+    if (r != PARAMENT_STATUS_SUCCESS) return r;
+    SplitArgs a;
+    double c0[2];
+    std::vector<double> mu;
+    split_coefficients(M, h * c->hnorm, c->hnorm, c0, mu);
+    a.c0 = make_double2(c0[0], c0[1]);
+    for (int n = 0; n <= kSplitMaxOrder; ++n)
+        a.mu[n] = (n >= 1 && n <= M) ? make_double2(mu[2 * n], mu[2 * n + 1]) : make_double2(0, 0);
+    a.stack = static_cast<const float4 *>(c->split_stack.ptr);
+    a.carr = static_cast<const float2 *>(d_carr);
+    a.P = P;
+    a.d = d;
+    a.Ke = (int)c->Ke;
+    a.M = M;
+    a.pts = pts;
+    a.K = (int)c->K;
+    a.amps = (int)amps;
+    a.mode = c->quad;
+    a.magnus = c->magnus ? 1 : 0;
+    a.hfac = h / 12.0;
+    const void *fn = pick_split(d);
+    const size_t smem = split_smem(d, (int)c->Ke);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem);
+    if (e != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        return PARAMENT_STATUS_CUBLAS_FAILED;
+    }
+    a.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)per_sm * c->num_sms, P));
+    const size_t dd = (size_t)d * d;
+    if (c->chunks.ensure(sizeof(double2) * dd * a.nchunks) != cudaSuccess ||
+        c->work.ensure(sizeof(double2) * dd * a.nchunks) != cudaSuccess ||
+        c->aux.ensure(sizeof(double2) * dd) != cudaSuccess)
+        return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+    a.chunks = static_cast<double2 *>(c->chunks.ptr);
+    void *args[] = {&a};
+    if (c->timing) cudaEventRecord(c->ev_start, stream);
+    e = cudaLaunchKernel(fn, dim3(a.nchunks), dim3(256), args, smem, stream);
+    if (c->timing) cudaEventRecord(c->ev_stop, stream);
+    int levels = 0;
+    if (e == cudaSuccess)
+        e = tree_product(true, d, c->chunks.ptr, a.nchunks, c->work.ptr, c->aux.ptr, stream, c->num_sms, &levels);
+    if (e == cudaSuccess) {
+        k_c128_to_c64<<<(int)((dd + 255) / 256), 256, 0, stream>>>(static_cast<const double2 *>(c->aux.ptr),
+                                                                   static_cast<float2 *>(d_out), (int)dd);
+        e = cudaGetLastError();
+    }
+    c->launches = 2 + levels;
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return PARAMENT_STATUS_CUBLAS_FAILED;
+    }
+    return PARAMENT_STATUS_SUCCESS;
 }
 
 }  // namespace pgb
