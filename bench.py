@@ -161,10 +161,11 @@ def flops_per_step(d, M, Ke, form):
 
 
 def split_products(M):
-    # Y = A^2, then powers Y^2..Y^((M-1)/2) as needed, one odd-part product and
-    # the running product.
+    """d^3 complex products per step of the split form: X^2 as hi*hi plus the
+    two cross products, the even powers X^4..X^(M-1), the odd part X*Q and
+    the running product."""
     q = (M - 1) // 2
-    return 1 + max(0, q - 1) + 1 + 1
+    return 3 + max(0, q - 1) + 1 + 1
 
 
 def run_form(torch, parament, w, form, K, W, flush, stream):

@@ -24,6 +24,7 @@ struct GemmArgs {
     cplx_t<R> alpha, diag;
     R beta;
     int d, batch, tiles_per_row;
+    int a_minus_identity;  // load A - I instead of A
 };
 
 template <class R, int BT>
@@ -49,7 +50,9 @@ __global__ void __launch_bounds__(256) k_gemm(const __grid_constant__ GemmArgs<R
             for (int t = tid; t < BT * BK; t += 256) {
                 int i = t / BK, kk = t % BK;
                 int r = r0 + i, k = k0 + kk;
-                As[i][kk] = (r < d && k < d) ? A[(size_t)r * d + k] : mk<C>(0.0, 0.0);
+                C v = (r < d && k < d) ? A[(size_t)r * d + k] : mk<C>(0.0, 0.0);
+                if (g.a_minus_identity && r == k && r < d) v.x -= (R)1;
+                As[i][kk] = v;
             }
             for (int t = tid; t < BT * BK; t += 256) {
                 int kk = t / BT, j = t % BT;
@@ -110,6 +113,7 @@ static cudaError_t run_gemm(const GemmLaunch &l) {
     g.d = l.d;
     g.batch = l.batch;
     g.tiles_per_row = (l.d + BT - 1) / BT;
+    g.a_minus_identity = l.a_minus_identity ? 1 : 0;
     dim3 grid(g.tiles_per_row * g.tiles_per_row, std::min(l.batch, 65535));
     k_gemm<R, BT><<<grid, 256, 0, l.stream>>>(g);
     return cudaGetLastError();
@@ -146,11 +150,17 @@ cudaError_t tree_product(bool fp64, int d, void *in, long long n, void *work, vo
         g.fp64 = fp64;
         g.d = d;
         g.batch = (int)pairs;
-        g.A = cur + dd * es;  // U_(2i+1): the later factor stands on the left
+        // W_i = U_(2i+1) U_(2i) (the later factor on the left), formed as
+        // U_(2i) + (U_(2i+1) - I) U_(2i) so that near-identity factors do not
+        // round their small terms against the unit diagonal.
+        g.A = cur + dd * es;
         g.strideA = 2 * dd;
+        g.a_minus_identity = true;
         g.B = cur;
         g.strideB = 2 * dd;
-        g.Cin = nullptr;
+        g.Cin = cur;
+        g.strideCin = 2 * dd;
+        g.beta = 1.0;
         g.Cout = nxt;
         g.strideCout = dd;
         g.alpha_re = 1.0;

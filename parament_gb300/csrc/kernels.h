@@ -64,6 +64,7 @@ struct GemmLaunch {
     double diag_re, diag_im;
     cudaStream_t stream;
     int num_sms;
+    bool a_minus_identity;  // use A - I in place of A
 };
 cudaError_t launch_gemm(const GemmLaunch &g);
 

@@ -146,11 +146,19 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
                     if (own[i][j]) Ps[eo[i][j]] = acc[i][j];
             __syncthreads();
         } else {
+            // U P = P + (U - I) P: the near-identity factor enters the sums
+            // without its unit diagonal, so sequential accumulation does not
+            // round small contributions against 1 (that bias adds up
+            // coherently over thousands of steps in FP32).
 #pragma unroll
             for (int i = 0; i < TM; ++i)
 #pragma unroll
                 for (int j = 0; j < TM; ++j)
-                    if (own[i][j]) Bs[eo[i][j]] = acc[i][j];
+                    if (own[i][j]) {
+                        C u = acc[i][j];
+                        if (diag[i][j]) u.x -= (R)1;
+                        Bs[eo[i][j]] = u;
+                    }
             __syncthreads();
             tile_gemm<C, TM>(acc, Bs, Ps, d, ty, tx);
             __syncthreads();
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
             for (int i = 0; i < TM; ++i)
 #pragma unroll
                 for (int j = 0; j < TM; ++j)
-                    if (own[i][j]) Ps[eo[i][j]] = acc[i][j];
+                    if (own[i][j]) Ps[eo[i][j]] = cadd(Ps[eo[i][j]], acc[i][j]);
             __syncthreads();
         }
     }
