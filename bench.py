@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--steps-per-prop", type=int, default=65536, help="time steps of the workload")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--forms", default="plain_c128,plain_c64,split_c64",
+                   help="comma-separated forms to measure (plain_c128 is the error reference)")
     return p.parse_args()
 
 
@@ -277,10 +279,16 @@ def run_ours(args, rank, world, local):
     from parament_gb300 import workloads
 
     w = workloads.magnus_d64(args.steps_per_prop)
+    # Inputs rounded to complex64 once, so every form sees identical values and
+    # the error column measures arithmetic only.
+    for k in ("H0", "H1", "carr"):
+        w[k] = w[k].astype(np.complex64).astype(np.complex128)
     P = w["P"]
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    forms = ["plain_c128", "plain_c64", "split_c64"]
+    forms = args.forms.split(",")
+    if "plain_c128" not in forms:
+        forms = ["plain_c128"] + forms
     res = {}
     for f in forms:
         try:

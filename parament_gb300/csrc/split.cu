@@ -235,14 +235,25 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
             for (int j = 0; j < TM; ++j) {
                 if (!own[i][j]) continue;
                 const int e = eo[i][j];
+                // Controls (slots < K): FP64 weights as float pairs times
+                // matrices that are exact in float, accumulated in
+                // double-float.  Magnus commutator slots carry weights of
+                // order dt |du| and stay in FP32: their rounding is far below
+                // the error bar even when it repeats at every step.
                 float4 h = a.stack[e];
                 cdf x = {{h.x, h.z}, {h.y, h.w}};
+                float2 small = make_float2(0.f, 0.f);
                 for (int m = 0; m < a.Ke; ++m) {
                     float4 g = a.stack[(size_t)(m + 1) * dd + e];
                     double2 w = ws[m];
-                    cdf wd = {df_from(w.x), df_from(w.y)};
-                    x = cdf_add(x, cdf_mul(wd, cdf{{g.x, g.z}, {g.y, g.w}}));
+                    if (m < a.K) {
+                        cdf wd = {df_from(w.x), df_from(w.y)};
+                        x = cdf_add(x, cdf_mul(wd, cdf{{g.x, g.z}, {g.y, g.w}}));
+                    } else {
+                        cfma(small, make_float2((float)w.x, (float)w.y), make_float2(g.x, g.y));
+                    }
                 }
+                x = cdf_add_c(x, small);
                 Xh[e] = cdf_hi(x);
                 Xl[e] = cdf_lo(x);
                 cdf v = cdf_mul(mu1, x);
