@@ -152,7 +152,7 @@ __device__ double2 split_weight(const SplitArgs &a, int m, long long s) {
 template <int TM, bool TWO>
 __device__ __forceinline__ void tile_gemm_f(float2 (&acc)[TM][TM], const float2 *__restrict__ A,
                                             const float2 *__restrict__ B, const float2 *__restrict__ A2,
-                                            const float2 *__restrict__ B2, int d, int ty, int tx) {
+                                            const float2 *__restrict__ B2, int d, int ld, int ty, int tx) {
 #pragma unroll
     for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -160,7 +160,7 @@ __device__ __forceinline__ void tile_gemm_f(float2 (&acc)[TM][TM], const float2 
     int ro[TM], co[TM];
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
-        ro[i] = min(ty + 16 * i, d - 1) * d;
+        ro[i] = min(ty + 16 * i, d - 1) * ld;
         co[i] = min(tx + 16 * i, d - 1);
     }
 #pragma unroll 4
@@ -169,7 +169,7 @@ __device__ __forceinline__ void tile_gemm_f(float2 (&acc)[TM][TM], const float2 
 #pragma unroll
         for (int i = 0; i < TM; ++i) av[i] = A[ro[i] + k];
 #pragma unroll
-        for (int j = 0; j < TM; ++j) bv[j] = B[k * d + co[j]];
+        for (int j = 0; j < TM; ++j) bv[j] = B[k * ld + co[j]];
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -178,7 +178,7 @@ __device__ __forceinline__ void tile_gemm_f(float2 (&acc)[TM][TM], const float2 
 #pragma unroll
             for (int i = 0; i < TM; ++i) av[i] = A2[ro[i] + k];
 #pragma unroll
-            for (int j = 0; j < TM; ++j) bv[j] = B2[k * d + co[j]];
+            for (int j = 0; j < TM; ++j) bv[j] = B2[k * ld + co[j]];
 #pragma unroll
             for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -187,22 +187,21 @@ __device__ __forceinline__ void tile_gemm_f(float2 (&acc)[TM][TM], const float2 
     }
 }
 
-__device__ __forceinline__ float2 cmulf_d(double2 mu, float2 g) {
-    // float product of a FP64 coefficient (rounded) and a float value.
-    return cmul(make_float2((float)mu.x, (float)mu.y), g);
-}
 
 template <int TM>
 __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ SplitArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int d = a.d, dd = d * d;
+    // Shared-memory matrices use row stride ld = d + 1 (bank-conflict free A reads).
+    const int d = a.d, dd = d * d, ld = d + 1, sz = d * ld;
     float2 *Xh = reinterpret_cast<float2 *>(smem_raw);  // X hi
-    float2 *Xl = Xh + dd;                               // X lo, later Q (odd part)
-    float2 *G2 = Xl + dd;                               // X^2, later E hi
-    float2 *Gc = G2 + dd;                               // X^(2k)
-    float2 *Ph = Gc + dd;                               // E^P hi
-    float2 *Pl = Ph + dd;                               // E^P lo
-    double2 *ws = reinterpret_cast<double2 *>(Pl + dd); // step weights
+    float2 *Xl = Xh + sz;                               // X lo, later Q (odd part)
+    float2 *G2 = Xl + sz;                               // X^2, later E hi
+    float2 *Gc = G2 + sz;                               // X^(2k)
+    float2 *Ph = Gc + sz;                               // E^P hi
+    float2 *Pl = Ph + sz;                               // E^P lo
+    float4 *ws = reinterpret_cast<float4 *>(Pl + sz);   // step weights (re_hi, re_lo, im_hi, im_lo)
+    __shared__ float2 muf[kSplitMaxOrder + 1];          // mu_n rounded to float (orders >= 3)
+    if (threadIdx.x <= kSplitMaxOrder) muf[threadIdx.x] = make_float2((float)a.mu[threadIdx.x].x, (float)a.mu[threadIdx.x].y);
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const long long s0 = a.P * blockIdx.x / a.nchunks;
     const long long s1 = a.P * (blockIdx.x + 1) / a.nchunks;
@@ -216,7 +215,7 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
         for (int j = 0; j < TM; ++j) {
             int r = ty + 16 * i, c = tx + 16 * j;
             own[i][j] = r < d && c < d;
-            eo[i][j] = r * d + c;
+            eo[i][j] = r * ld + c;
             dg[i][j] = r == c;
         }
     const cdf mu1 = {df_from(a.mu[1].x), df_from(a.mu[1].y)};
@@ -226,7 +225,11 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
     cdf E[TM][TM];
     float2 acc[TM][TM], Q[TM][TM];
     for (long long st = s0; st < s1; ++st) {
-        for (int m = tid; m < a.Ke; m += blockDim.x) ws[m] = split_weight(a, m, st);
+        for (int m = tid; m < a.Ke; m += blockDim.x) {
+            double2 w = split_weight(a, m, st);
+            df re = df_from(w.x), im = df_from(w.y);
+            ws[m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        }
         __syncthreads();
         // X = H0 + sum_m w_m H_m in double-float; E starts as (m_0-1) I + mu_1 X.
 #pragma unroll
@@ -235,22 +238,23 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
             for (int j = 0; j < TM; ++j) {
                 if (!own[i][j]) continue;
                 const int e = eo[i][j];
+                const int ge = (ty + 16 * i) * d + tx + 16 * j;
                 // Controls (slots < K): FP64 weights as float pairs times
                 // matrices that are exact in float, accumulated in
                 // double-float.  Magnus commutator slots carry weights of
                 // order dt |du| and stay in FP32: their rounding is far below
                 // the error bar even when it repeats at every step.
-                float4 h = a.stack[e];
+                float4 h = a.stack[ge];
                 cdf x = {{h.x, h.z}, {h.y, h.w}};
                 float2 small = make_float2(0.f, 0.f);
                 for (int m = 0; m < a.Ke; ++m) {
-                    float4 g = a.stack[(size_t)(m + 1) * dd + e];
-                    double2 w = ws[m];
+                    float4 g = a.stack[(size_t)(m + 1) * dd + ge];
+                    float4 w = ws[m];
                     if (m < a.K) {
-                        cdf wd = {df_from(w.x), df_from(w.y)};
+                        cdf wd = {{w.x, w.y}, {w.z, w.w}};
                         x = cdf_add(x, cdf_mul(wd, cdf{{g.x, g.z}, {g.y, g.w}}));
                     } else {
-                        cfma(small, make_float2((float)w.x, (float)w.y), make_float2(g.x, g.y));
+                        cfma(small, make_float2(w.x, w.z), make_float2(g.x, g.y));
                     }
                 }
                 x = cdf_add_c(x, small);
@@ -262,10 +266,10 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
             }
         __syncthreads();
         // G2 = X^2 = Xh Xh + (Xh Xl + Xl Xh).
-        tile_gemm_f<TM, false>(acc, Xh, Xh, nullptr, nullptr, d, ty, tx);
+        tile_gemm_f<TM, false>(acc, Xh, Xh, nullptr, nullptr, d, ld, ty, tx);
         {
             float2 cr[TM][TM];
-            tile_gemm_f<TM, true>(cr, Xh, Xl, Xl, Xh, d, ty, tx);
+            tile_gemm_f<TM, true>(cr, Xh, Xl, Xl, Xh, d, ld, ty, tx);
 #pragma unroll
             for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -277,23 +281,23 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
             for (int j = 0; j < TM; ++j) {
                 if (!own[i][j]) continue;
                 E[i][j] = cdf_add(E[i][j], cdf_mul_c(mu2, acc[i][j]));
-                Q[i][j] = (M >= 3) ? cmulf_d(a.mu[3], acc[i][j]) : make_float2(0.f, 0.f);
+                Q[i][j] = (M >= 3) ? cmul(muf[3], acc[i][j]) : make_float2(0.f, 0.f);
                 G2[eo[i][j]] = acc[i][j];
                 Gc[eo[i][j]] = acc[i][j];
             }
         __syncthreads();
         // Higher even powers X^(2k) = X^(2k-2) X^2 in FP32.
         for (int k = 2; 2 * k <= M; ++k) {
-            tile_gemm_f<TM, false>(acc, Gc, G2, nullptr, nullptr, d, ty, tx);
+            tile_gemm_f<TM, false>(acc, Gc, G2, nullptr, nullptr, d, ld, ty, tx);
             __syncthreads();
 #pragma unroll
             for (int i = 0; i < TM; ++i)
 #pragma unroll
                 for (int j = 0; j < TM; ++j) {
                     if (!own[i][j]) continue;
-                    E[i][j] = cdf_add_c(E[i][j], cmulf_d(a.mu[2 * k], acc[i][j]));
+                    E[i][j] = cdf_add_c(E[i][j], cmul(muf[2 * k], acc[i][j]));
                     if (2 * k + 1 <= M) {
-                        float2 q = cmulf_d(a.mu[2 * k + 1], acc[i][j]);
+                        float2 q = cmul(muf[2 * k + 1], acc[i][j]);
                         Q[i][j] = make_float2(Q[i][j].x + q.x, Q[i][j].y + q.y);
                     }
                     Gc[eo[i][j]] = acc[i][j];
@@ -307,7 +311,7 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
             for (int j = 0; j < TM; ++j)
                 if (own[i][j]) Xl[eo[i][j]] = Q[i][j];
         __syncthreads();
-        tile_gemm_f<TM, false>(acc, Xh, Xl, nullptr, nullptr, d, ty, tx);
+        tile_gemm_f<TM, false>(acc, Xh, Xl, nullptr, nullptr, d, ld, ty, tx);
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -333,7 +337,7 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
                 for (int j = 0; j < TM; ++j)
                     if (own[i][j]) G2[eo[i][j]] = cdf_hi(E[i][j]);
             __syncthreads();
-            tile_gemm_f<TM, false>(acc, G2, Ph, nullptr, nullptr, d, ty, tx);
+            tile_gemm_f<TM, false>(acc, G2, Ph, nullptr, nullptr, d, ld, ty, tx);
             __syncthreads();
 #pragma unroll
             for (int i = 0; i < TM; ++i)
@@ -354,7 +358,8 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
     if (s1 > s0) {
         double2 *dst = a.chunks + (size_t)blockIdx.x * dd;
         for (int e = tid; e < dd; e += blockDim.x) {
-            float2 ph = Ph[e], pl = Pl[e];
+            const int se = (e / d) * ld + e % d;
+            float2 ph = Ph[se], pl = Pl[se];
             double re = (double)ph.x + (double)pl.x, im = (double)ph.y + (double)pl.y;
             if (e / d == e % d) re += 1.0;
             dst[e] = make_double2(re, im);
@@ -380,7 +385,7 @@ __global__ void k_c64_to_c128(const float2 *src, double2 *dst, long long n) {
         dst[i] = make_double2(src[i].x, src[i].y);
 }
 
-static size_t split_smem(int d, int Ke) { return 6 * (size_t)d * d * sizeof(float2) + (size_t)std::max(Ke, 1) * 16; }
+static size_t split_smem(int d, int Ke) { return 6 * (size_t)d * (d + 1) * sizeof(float2) + (size_t)std::max(Ke, 1) * 16; }
 
 template <int TM>
 static const void *split_kernel_ptr() {

@@ -31,10 +31,11 @@ struct SmallArgs {
 
 // acc[i][j] = sum_k A[r_i][k] B[k][c_j] for the thread's TM x TM micro-tile,
 // rows r_i = ty + 16 i, columns c_j = tx + 16 j (rows/cols past d are clamped
-// reads whose results the caller discards).
+// reads whose results the caller discards).  Shared-memory matrices have row
+// stride ld = d + 1, so the two rows a warp reads of A sit in different banks.
 template <class C, int TM>
 __device__ __forceinline__ void tile_gemm(C (&acc)[TM][TM], const C *__restrict__ A, const C *__restrict__ B, int d,
-                                          int ty, int tx) {
+                                          int ld, int ty, int tx) {
 #pragma unroll
     for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -42,7 +43,7 @@ __device__ __forceinline__ void tile_gemm(C (&acc)[TM][TM], const C *__restrict_
     int ro[TM], co[TM];
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
-        ro[i] = min(ty + 16 * i, d - 1) * d;
+        ro[i] = min(ty + 16 * i, d - 1) * ld;
         co[i] = min(tx + 16 * i, d - 1);
     }
 #pragma unroll 4
@@ -51,7 +52,7 @@ __device__ __forceinline__ void tile_gemm(C (&acc)[TM][TM], const C *__restrict_
 #pragma unroll
         for (int i = 0; i < TM; ++i) a[i] = A[ro[i] + k];
 #pragma unroll
-        for (int j = 0; j < TM; ++j) b[j] = B[k * d + co[j]];
+        for (int j = 0; j < TM; ++j) b[j] = B[k * ld + co[j]];
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -59,15 +60,16 @@ __device__ __forceinline__ void tile_gemm(C (&acc)[TM][TM], const C *__restrict_
     }
 }
 
+// Complex64 instances keep to 128 registers so that two CTAs share an SM.
 template <class R, int TM>
-__global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ SmallArgs<R> a) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_small_steps(const __grid_constant__ SmallArgs<R> a) {
     using C = cplx_t<R>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int d = a.d, dd = d * d;
+    const int d = a.d, dd = d * d, ld = d + 1, sz = d * ld;
     C *Xs = reinterpret_cast<C *>(smem_raw);
-    C *Bs = Xs + dd;
-    C *Ps = Bs + dd;
-    C *ws = Ps + dd;
+    C *Bs = Xs + sz;
+    C *Ps = Bs + sz;
+    C *ws = Ps + sz;
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const long long s0 = a.P * blockIdx.x / a.nchunks;
     const long long s1 = a.P * (blockIdx.x + 1) / a.nchunks;
@@ -75,7 +77,7 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
     const R s = a.s;
 
     bool own[TM][TM];
-    int eo[TM][TM];
+    int eo[TM][TM];  // shared-memory index (stride ld); the global index is r*d+c
     bool diag[TM][TM];
 #pragma unroll
     for (int i = 0; i < TM; ++i)
@@ -83,7 +85,7 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
         for (int j = 0; j < TM; ++j) {
             int r = ty + 16 * i, c = tx + 16 * j;
             own[i][j] = (r < d) && (c < d);
-            eo[i][j] = r * d + c;
+            eo[i][j] = r * ld + c;
             diag[i][j] = (r == c);
         }
 
@@ -100,8 +102,9 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
             for (int j = 0; j < TM; ++j) {
                 if (!own[i][j]) continue;
                 const int e = eo[i][j];
-                C v = a.stack[e];
-                for (int m = 0; m < a.Ke; ++m) cfma(v, ws[m], a.stack[(size_t)(m + 1) * dd + e]);
+                const int ge = (ty + 16 * i) * d + tx + 16 * j;
+                C v = a.stack[ge];
+                for (int m = 0; m < a.Ke; ++m) cfma(v, ws[m], a.stack[(size_t)(m + 1) * dd + ge]);
                 Xs[e] = v;
                 C bm1 = cscale(cmul(a.J[M], v), s);
                 if (diag[i][j]) bm1 = cadd(bm1, a.J[M - 1]);
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
         if (M > 1) {
             __syncthreads();
             for (int k = M - 2; k >= 0; --k) {
-                tile_gemm<C, TM>(acc, Bs, Xs, d, ty, tx);
+                tile_gemm<C, TM>(acc, Bs, Xs, d, ld, ty, tx);
                 __syncthreads();
                 const R beta = (k == 0) ? (R)-2 : (R)-1;
 #pragma unroll
@@ -160,7 +163,7 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
                         Bs[eo[i][j]] = u;
                     }
             __syncthreads();
-            tile_gemm<C, TM>(acc, Bs, Ps, d, ty, tx);
+            tile_gemm<C, TM>(acc, Bs, Ps, d, ld, ty, tx);
             __syncthreads();
 #pragma unroll
             for (int i = 0; i < TM; ++i)
@@ -172,13 +175,13 @@ __global__ void __launch_bounds__(256) k_small_steps(const __grid_constant__ Sma
     }
     if (s1 > s0) {
         C *dst = a.chunks + (size_t)blockIdx.x * dd;
-        for (int e = tid; e < dd; e += blockDim.x) dst[e] = Ps[e];
+        for (int e = tid; e < dd; e += blockDim.x) dst[e] = Ps[(e / d) * ld + e % d];
     }
 }
 
 size_t small_smem_bytes(bool fp64, int d, int Ke) {
     size_t c = fp64 ? 16 : 8;
-    return c * (3 * (size_t)d * d + (size_t)Ke);
+    return c * (3 * (size_t)d * (d + 1) + (size_t)Ke);
 }
 
 template <class R, int TM>
