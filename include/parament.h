@@ -58,7 +58,8 @@ typedef enum Parament_ErrorCode {
     PARAMENT_STATUS_NO_HAMILTONIAN = 80,
     PARAMENT_STATUS_INVALID_QUADRATURE_SELECTION = 90,
     PARAMENT_FAIL = 1000,
-    PARAMENT_STATUS_KERNEL_TIMEOUT = 1010 /* a bounded device-side wait gave up (batched queue) */
+    PARAMENT_STATUS_KERNEL_TIMEOUT = 1010, /* a bounded device-side wait gave up (batched queue) */
+    PARAMENT_STATUS_SCRATCH_EXCEEDED = 1020 /* problem larger than Parament_equipropNoAlloc_fp64's fixed scratch */
 } Parament_ErrorCode;
 
 /* ---------------------------------------------------------------- reference ABI */
@@ -152,6 +153,23 @@ PARAMENT_API Parament_ErrorCode Parament_equipropDevice(Parament_Context_f32 *ha
 PARAMENT_API Parament_ErrorCode Parament_equipropDevice_fp64(Parament_Context_f64 *handle, const void *d_carr,
                                                              double dt, unsigned int pts, unsigned int amps,
                                                              void *d_out, void *stream);
+
+/* equiprop that allocates no device memory (no counterpart in the reference).
+ * For callers that must not call cudaMalloc while they propagate: real-time
+ * loops that cannot wait on the allocator, applications whose device memory
+ * belongs to their own pool, plug-ins where runtime allocation is forbidden.
+ * The Hamiltonian must be loaded beforehand (Parament_setHamiltonian_fp64
+ * allocates once, at set-up); d_carr and d_out are the caller's device
+ * buffers; the work goes to `stream` (NULL: the context's stream) and the call
+ * returns without waiting.  Scratch lives in a fixed 24 MiB device array inside
+ * the library (held on each GPU that loads it until exit).  Limits: complex128
+ * contexts with dim <= 64; larger problems return
+ * PARAMENT_STATUS_SCRATCH_EXCEEDED.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) -- make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race; serialise them. */
+PARAMENT_API Parament_ErrorCode Parament_equipropNoAlloc_fp64(Parament_Context_f64 *handle, const void *d_carr,
+                                                              double dt, unsigned int pts, unsigned int amps,
+                                                              void *d_out, void *stream);
 
 /* Instrumentation (new).  With timing enabled, each equiprop records CUDA
  * events on its stream around its dominant kernel (the fused step kernel, or

@@ -476,6 +476,8 @@ const char *Parament_errorMessage(Parament_ErrorCode errorCode) {
         case PARAMENT_STATUS_INVALID_QUADRATURE_SELECTION: return "Invalid quadrature selection.";
         case PARAMENT_STATUS_NO_HAMILTONIAN: return "No hamiltonian set";
         case PARAMENT_STATUS_KERNEL_TIMEOUT: return "A bounded device-side wait timed out.";
+        case PARAMENT_STATUS_SCRATCH_EXCEEDED:
+            return "Problem too large for the fixed scratch of the no-allocation entry point (complex128, dim <= 64).";
         default: return "Unknown error code";
     }
 }
