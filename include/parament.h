@@ -154,6 +154,30 @@ PARAMENT_API Parament_ErrorCode Parament_equipropDevice_fp64(Parament_Context_f6
                                                              double dt, unsigned int pts, unsigned int amps,
                                                              void *d_out, void *stream);
 
+/* Adjoint gradient (new; no reference counterpart).  For a seed W (d x d,
+ * row-major) returns, for every real control sample,
+ *     grad[k*pts + i] = d/du_k[i]  Re Tr(W^H U),
+ * U the propagator equiprop would return for the same arguments (the exact
+ * derivative of the computed Chebyshev propagator, including the quadrature
+ * and Magnus weights).  A loss L(U) with dL = Re Tr(G^H dU) has dL/du = grad
+ * for W = G; for L = 1 - |Tr(V^H U)|^2 / d^2 use W = -(2/d^2) Tr(V^H U) V.
+ * Controls are taken as real: the imaginary parts of the samples enter U but
+ * get no derivative.  grad is float for complex64 contexts and double for
+ * complex128 ones.  Limits: dim <= 64 (complex64) or 48 (complex128).
+ * Memory: one d x d checkpoint per step plus Ke traces per step. */
+PARAMENT_API Parament_ErrorCode Parament_equipropVJP(Parament_Context_f32 *handle, cuComplex *carr, double dt,
+                                                     unsigned int pts, unsigned int amps, cuComplex *W, float *grad);
+PARAMENT_API Parament_ErrorCode Parament_equipropVJP_fp64(Parament_Context_f64 *handle, cuDoubleComplex *carr,
+                                                          double dt, unsigned int pts, unsigned int amps,
+                                                          cuDoubleComplex *W, double *grad);
+/* Same on device buffers, queued on `stream` (NULL: the context's stream). */
+PARAMENT_API Parament_ErrorCode Parament_equipropVJPDevice(Parament_Context_f32 *handle, const void *d_carr, double dt,
+                                                           unsigned int pts, unsigned int amps, const void *d_W,
+                                                           void *d_grad, void *stream);
+PARAMENT_API Parament_ErrorCode Parament_equipropVJPDevice_fp64(Parament_Context_f64 *handle, const void *d_carr,
+                                                                double dt, unsigned int pts, unsigned int amps,
+                                                                const void *d_W, void *d_grad, void *stream);
+
 /* equiprop that allocates no device memory (no counterpart in the reference).
  * For callers that must not call cudaMalloc while they propagate: real-time
  * loops that cannot wait on the allocator, applications whose device memory

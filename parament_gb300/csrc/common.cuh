@@ -110,4 +110,48 @@ __device__ __forceinline__ C step_weight(const C *__restrict__ carr, const Weigh
     return cmul(t, f);
 }
 
+// acc[i][j] = sum_k A[r_i][k] B[k][c_j] (plus A2[r_i][k] B2[k][c_j] when A2 is
+// given) for a thread's TM x TM micro-tile of a d x d product held in shared
+// memory: 256 threads as 16 x 16, rows r_i = ty + 16 i, columns
+// c_j = tx + 16 j.  Rows/columns past d are clamped reads whose results the
+// caller discards.  Shared-memory matrices have row stride ld = d + 1, so the
+// two rows a warp reads of A sit in different banks.
+template <class C, int TM>
+__device__ __forceinline__ void tile_gemm(C (&acc)[TM][TM], const C *__restrict__ A, const C *__restrict__ B, int d,
+                                          int ld, int ty, int tx, const C *__restrict__ A2 = nullptr,
+                                          const C *__restrict__ B2 = nullptr) {
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TM; ++j) acc[i][j] = mk<C>(0.0, 0.0);
+    int ro[TM], co[TM];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        ro[i] = min(ty + 16 * i, d - 1) * ld;
+        co[i] = min(tx + 16 * i, d - 1);
+    }
+#pragma unroll 4
+    for (int k = 0; k < d; ++k) {
+        C a[TM], b[TM];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) a[i] = A[ro[i] + k];
+#pragma unroll
+        for (int j = 0; j < TM; ++j) b[j] = B[k * ld + co[j]];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j) cfma(acc[i][j], a[i], b[j]);
+        if (A2) {
+#pragma unroll
+            for (int i = 0; i < TM; ++i) a[i] = A2[ro[i] + k];
+#pragma unroll
+            for (int j = 0; j < TM; ++j) b[j] = B2[k * ld + co[j]];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) cfma(acc[i][j], a[i], b[j]);
+        }
+    }
+}
+
 }  // namespace pgb

@@ -54,7 +54,7 @@ struct Ctx {
     int launches = 0;
 
     // Work buffers (grow-only, like src/cuda/parament.cpp:418-474)
-    DevBuf carr, out, chunks, work, X, B1, B2, aux;
+    DevBuf carr, out, chunks, work, X, B1, B2, aux, grad;
 
     size_t esize() const { return fp64 ? 16 : 8; }
     void release_all() {
@@ -68,6 +68,7 @@ struct Ctx {
         B1.release();
         B2.release();
         aux.release();
+        grad.release();
     }
 };
 
@@ -80,5 +81,10 @@ long long num_steps(int quad, bool magnus, unsigned pts);
 int split_order(double hnorm, double h, long long P);
 Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned amps, double h, int M, long long P,
                              void *d_out, cudaStream_t stream);
+
+// Adjoint: d/du_k[i] Re Tr(W^H U) for real samples, d <= adj_max_dim.
+int adj_max_dim(bool fp64);
+Parament_ErrorCode run_vjp(Ctx *c, const void *d_carr, double dt, unsigned pts, unsigned amps, const void *d_W,
+                           void *d_grad, cudaStream_t stream);
 
 }  // namespace pgb

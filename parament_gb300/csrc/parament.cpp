@@ -550,6 +550,66 @@ Parament_ErrorCode Parament_equipropDevice_fp64(Parament_Context_f64 *handle, co
                                            stream ? static_cast<cudaStream_t>(stream) : c->stream);
 }
 
+static Parament_ErrorCode vjp_host(Ctx *c, const void *carr, double dt, unsigned pts, unsigned amps, const void *W,
+                                   void *grad) {
+    cudaSetDevice(c->device);
+    if (!c->has_h) return c->last_error = PARAMENT_STATUS_NO_HAMILTONIAN;
+    if (!W || !grad || (amps > 0 && !carr)) return c->last_error = PARAMENT_STATUS_INVALID_VALUE;
+    const size_t es = c->esize(), dd = (size_t)c->dim * c->dim;
+    const size_t cbytes = es * (size_t)amps * pts, gbytes = (es / 2) * (size_t)amps * pts;
+    if (c->carr.ensure(std::max<size_t>(cbytes, 16)) != cudaSuccess || c->out.ensure(es * dd) != cudaSuccess ||
+        c->grad.ensure(std::max<size_t>(gbytes, 16)) != cudaSuccess)
+        return c->last_error = PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+    cudaError_t e = cudaSuccess;
+    if (cbytes) e = cudaMemcpyAsync(c->carr.ptr, carr, cbytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->out.ptr, W, es * dd, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return c->last_error = PARAMENT_FAIL;
+    }
+    Parament_ErrorCode r = run_vjp(c, c->carr.ptr, dt, pts, amps, c->out.ptr, c->grad.ptr, c->stream);
+    if (r != PARAMENT_STATUS_SUCCESS) {
+        cudaStreamSynchronize(c->stream);
+        return c->last_error = r;
+    }
+    if (gbytes) e = cudaMemcpyAsync(grad, c->grad.ptr, gbytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return c->last_error = PARAMENT_STATUS_CUBLAS_FAILED;
+    }
+    return c->last_error = PARAMENT_STATUS_SUCCESS;
+}
+
+Parament_ErrorCode Parament_equipropVJP(Parament_Context_f32 *handle, cuComplex *carr, double dt, unsigned int pts,
+                                        unsigned int amps, cuComplex *W, float *grad) {
+    if (!handle) return PARAMENT_STATUS_INVALID_VALUE;
+    return vjp_host(as_ctx(handle), carr, dt, pts, amps, W, grad);
+}
+Parament_ErrorCode Parament_equipropVJP_fp64(Parament_Context_f64 *handle, cuDoubleComplex *carr, double dt,
+                                             unsigned int pts, unsigned int amps, cuDoubleComplex *W, double *grad) {
+    if (!handle) return PARAMENT_STATUS_INVALID_VALUE;
+    return vjp_host(as_ctx(handle), carr, dt, pts, amps, W, grad);
+}
+Parament_ErrorCode Parament_equipropVJPDevice(Parament_Context_f32 *handle, const void *d_carr, double dt,
+                                              unsigned int pts, unsigned int amps, const void *d_W, void *d_grad,
+                                              void *stream) {
+    if (!handle) return PARAMENT_STATUS_INVALID_VALUE;
+    Ctx *c = as_ctx(handle);
+    cudaSetDevice(c->device);
+    return c->last_error = run_vjp(c, d_carr, dt, pts, amps, d_W, d_grad,
+                                   stream ? static_cast<cudaStream_t>(stream) : c->stream);
+}
+Parament_ErrorCode Parament_equipropVJPDevice_fp64(Parament_Context_f64 *handle, const void *d_carr, double dt,
+                                                   unsigned int pts, unsigned int amps, const void *d_W, void *d_grad,
+                                                   void *stream) {
+    if (!handle) return PARAMENT_STATUS_INVALID_VALUE;
+    Ctx *c = as_ctx(handle);
+    cudaSetDevice(c->device);
+    return c->last_error = run_vjp(c, d_carr, dt, pts, amps, d_W, d_grad,
+                                   stream ? static_cast<cudaStream_t>(stream) : c->stream);
+}
+
 static Parament_ErrorCode set_timing(Ctx *c, int enable) {
     cudaSetDevice(c->device);
     if (enable && !c->ev_start) {

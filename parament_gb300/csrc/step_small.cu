@@ -29,37 +29,6 @@ struct SmallArgs {
     WeightSpec w;
 };
 
-// acc[i][j] = sum_k A[r_i][k] B[k][c_j] for the thread's TM x TM micro-tile,
-// rows r_i = ty + 16 i, columns c_j = tx + 16 j (rows/cols past d are clamped
-// reads whose results the caller discards).  Shared-memory matrices have row
-// stride ld = d + 1, so the two rows a warp reads of A sit in different banks.
-template <class C, int TM>
-__device__ __forceinline__ void tile_gemm(C (&acc)[TM][TM], const C *__restrict__ A, const C *__restrict__ B, int d,
-                                          int ld, int ty, int tx) {
-#pragma unroll
-    for (int i = 0; i < TM; ++i)
-#pragma unroll
-        for (int j = 0; j < TM; ++j) acc[i][j] = mk<C>(0.0, 0.0);
-    int ro[TM], co[TM];
-#pragma unroll
-    for (int i = 0; i < TM; ++i) {
-        ro[i] = min(ty + 16 * i, d - 1) * ld;
-        co[i] = min(tx + 16 * i, d - 1);
-    }
-#pragma unroll 4
-    for (int k = 0; k < d; ++k) {
-        C a[TM], b[TM];
-#pragma unroll
-        for (int i = 0; i < TM; ++i) a[i] = A[ro[i] + k];
-#pragma unroll
-        for (int j = 0; j < TM; ++j) b[j] = B[k * ld + co[j]];
-#pragma unroll
-        for (int i = 0; i < TM; ++i)
-#pragma unroll
-            for (int j = 0; j < TM; ++j) cfma(acc[i][j], a[i], b[j]);
-    }
-}
-
 // Complex64 instances keep to 128 registers so that two CTAs share an SM.
 template <class R, int TM>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_small_steps(const __grid_constant__ SmallArgs<R> a) {

@@ -256,6 +256,66 @@ class Parament:
         self._check_error(code)
         return out
 
+    @_must_be_alive
+    def vjp(self, dt, W, *carr):
+        """Vector-Jacobian product of :meth:`equiprop`: for a seed ``W`` (dim x dim)
+        returns ``grad`` with ``grad[k, i] = d/du_k[i] Re Tr(W^H U)`` for real
+        control samples.  A loss with ``dL = Re Tr(G^H dU)`` has ``dL/du = grad``
+        for ``W = G``."""
+        if self.amps < 0:
+            raise RuntimeError("No hamiltonian set")
+        amps = len(carr)
+        if amps > self.amps:
+            raise ValueError(f'Got {amps} amplitude arrays, but there are only {self.amps} Hamiltonians.')
+        pts = np.shape(carr[0])[0] if amps else 0
+        if any(np.shape(c) != (pts,) for c in carr):
+            raise ValueError("All amplitude arrays must have the same length.")
+        samples = np.ascontiguousarray(np.asarray(carr, dtype=self._ctype).reshape(amps, pts).ravel())
+        if samples.size == 0:
+            samples = np.zeros(1, dtype=self._ctype)
+        w = np.ascontiguousarray(np.asarray(W, dtype=self._ctype).reshape(self.dim, self.dim).ravel())
+        grad = np.zeros(max(amps * pts, 1), dtype=np.float64 if self._use_doubles else np.float32)
+        self._check_error(self._fn('Parament_equipropVJP')(self._handle, samples, float(dt), pts, amps, w, grad))
+        return grad[:amps * pts].reshape(amps, pts)
+
+    def fidelity_gradient(self, dt, U_target, *carr):
+        """Loss ``1 - |Tr(V^H U)|^2 / d^2`` for the target ``V = U_target`` and its
+        gradient with respect to every real control sample: ``(loss, grad)``."""
+        U = np.asarray(self.equiprop(dt, *carr), dtype=np.complex128)
+        V = np.asarray(U_target, dtype=np.complex128)
+        d = self.dim
+        g = np.trace(V.conj().T @ U)
+        loss = 1.0 - abs(g) ** 2 / d ** 2
+        W = -(2.0 / d ** 2) * g * V
+        return loss, self.vjp(dt, W, *carr)
+
+    @_must_be_alive
+    def vjp_device(self, dt, carr, W, grad=None, stream=None):
+        """:meth:`vjp` on CUDA tensors: ``carr`` (amps, pts) and ``W`` (dim, dim)
+        on the context's device; ``grad`` (amps, pts) real, allocated when None."""
+        import torch
+
+        ct = torch.complex128 if self._use_doubles else torch.complex64
+        rt = torch.float64 if self._use_doubles else torch.float32
+        carr = carr.to(ct)
+        if carr.dim() == 1:
+            carr = carr.unsqueeze(0)
+        carr = carr.contiguous()
+        W = W.to(ct).contiguous()
+        amps, pts = carr.shape
+        if amps > self.amps:
+            raise ValueError(f'Got {amps} amplitude arrays, but there are only {self.amps} Hamiltonians.')
+        if grad is None:
+            grad = torch.empty((amps, pts), dtype=rt, device=carr.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(carr.device)
+        code = self._fn('Parament_equipropVJPDevice')(self._handle, ctypes.c_void_p(carr.data_ptr()), float(dt),
+                                                      pts, amps, ctypes.c_void_p(W.data_ptr()),
+                                                      ctypes.c_void_p(grad.data_ptr()),
+                                                      ctypes.c_void_p(stream.cuda_stream))
+        self._check_error(code)
+        return grad
+
     # ------------------------------------------------------------------ errors
 
     @_must_be_alive

@@ -89,3 +89,10 @@ for _sfx in ("", "_fp64"):
     getattr(lib, "Parament_lastKernelMs" + _sfx).restype = ctypes.c_float
     getattr(lib, "Parament_lastLaunchCount" + _sfx).argtypes = [c_ParamentContext_p]
     getattr(lib, "Parament_lastLaunchCount" + _sfx).restype = ctypes.c_int
+lib.Parament_equipropVJP.argtypes = [c_ParamentContext_p, c_cuComplex_p, ctypes.c_double, ctypes.c_uint,
+                                     ctypes.c_uint, c_cuComplex_p, np.ctypeslib.ndpointer(np.float32)]
+lib.Parament_equipropVJP_fp64.argtypes = [c_ParamentContext_p, c_cuDoubleComplex_p, ctypes.c_double, ctypes.c_uint,
+                                          ctypes.c_uint, c_cuDoubleComplex_p, np.ctypeslib.ndpointer(np.float64)]
+for _name in ("Parament_equipropVJPDevice", "Parament_equipropVJPDevice_fp64"):
+    getattr(lib, _name).argtypes = [c_ParamentContext_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_uint,
+                                    ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
