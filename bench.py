@@ -33,7 +33,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "equiprop time steps/s (d=64 K=4 Magnus+Simpson, 65536 steps) at <=1e-6 rel err vs FP64"
+METRIC = ("equiprop time steps/s (d=64 K=4 Magnus+Simpson, 65536 steps) at <=1e-6 rel err vs FP64; "
+          "GRAPE grads/s in 'grape'")
 UNIT = "steps/s"
 L2_FLUSH_BYTES = 512 << 20
 
@@ -213,6 +214,67 @@ def run_form(torch, parament, w, form, K, W, flush, stream):
     es = 16 if precision == "fp64" else 8
     return {"ms": times, "kernel_ms": kms, "U": U, "M": M, "launches": launches, "e2e_s": e2e,
             "h2d": w["carr"].size * es, "d2h": 64 * 64 * es}
+
+
+def grape_block(torch, parament, K_steps, W_steps, flush, stream):
+    """GRAPE gradient workload: d=32, K=6, 16384 steps, complex64 context,
+    fidelity loss 1 - |Tr(V^H U)|^2/d^2 against a Haar-random target.  One
+    gradient = forward equiprop + adjoint VJP over all 98304 controls, device
+    resident.  Finite differences need 2 equiprops per control."""
+    from parament_gb300 import workloads
+    w = workloads.adjoint_d32()
+    for k in ("H0", "H1"):
+        w[k] = w[k].astype(np.complex64).astype(np.complex128)
+    carr_np = w["carr"].real.astype(np.float32).astype(np.float64)
+    V = workloads.haar_unitary(32, seed=1)
+    out = {}
+    grads = {}
+    for prec in ("fp32", "fp64"):
+        ctx = parament.Parament(prec)
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+        ct = torch.complex128 if prec == "fp64" else torch.complex64
+        carr = torch.tensor(carr_np, dtype=ct, device="cuda")
+        Vt = torch.tensor(V, dtype=ct, device="cuda")
+        U = torch.empty((32, 32), dtype=ct, device="cuda")
+
+        def one():
+            ctx.equiprop_device(w["dt"], carr, U, stream)
+            g = torch.trace(Vt.conj().T @ U)
+            Wt = (-(2.0 / 32 ** 2) * g) * Vt
+            return ctx.vjp_device(w["dt"], carr, Wt, stream=stream)
+
+        with torch.cuda.stream(stream):
+            for _ in range(W_steps):
+                one()
+            stream.synchronize()
+            ts = []
+            for _ in range(K_steps):
+                flush.zero_()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                gr = one()
+                e.record(stream)
+                ts.append((s, e))
+            stream.synchronize()
+            # one forward alone, for the finite-difference rate
+            fs, fe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            fs.record(stream)
+            for _ in range(3):
+                ctx.equiprop_device(w["dt"], carr, U, stream)
+            fe.record(stream)
+            stream.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ts) / len(ts)
+        t_fwd = fs.elapsed_time(fe) / 3
+        n = carr_np.size
+        grads[prec] = gr.double().cpu().numpy()
+        out[prec] = {"grads_per_s": round(n / (ms * 1e-3), 1), "ms_per_gradient": round(ms, 4),
+                     "fd_grads_per_s": round(1.0 / (2 * t_fwd * 1e-3), 1),
+                     "adjoint_over_fd": round((n / ms) / (1.0 / (2 * t_fwd)), 1)}
+        ctx.destroy()
+    out["fp32"]["rel_err_vs_fp64_gradient"] = float(np.linalg.norm(grads["fp32"] - grads["fp64"]) /
+                                                    np.linalg.norm(grads["fp64"]))
+    out["workload"] = "adjoint_d32_K6_16384steps fidelity loss, Haar target (seed 1), 98304 controls"
+    return out
 
 
 def cpu_baseline(w, target_s=10.0):
@@ -395,6 +457,10 @@ def run_ours(args, rank, world, local):
                      "pipe_peak_source": "cuBLAS GEMM 8192^3 measured in this run", **lib_peaks},
         "clocks": clk.summary(),
     }
+    try:
+        line["grape"] = grape_block(torch, parament, args.steps, args.warmup, flush, stream)
+    except (ValueError, RuntimeError) as e:
+        line["grape"] = {"error": str(e)}
     if not args.no_cpu_baseline:
         base, S, t = cpu_baseline(w)
         line["cpu_baseline"] = base

@@ -178,6 +178,31 @@ PARAMENT_API Parament_ErrorCode Parament_equipropVJPDevice_fp64(Parament_Context
                                                                 double dt, unsigned int pts, unsigned int amps,
                                                                 const void *d_W, void *d_grad, void *stream);
 
+/* Batched ensembles (new; no reference counterpart).  nprob independent
+ * problems, each with its own dim (<= 64), control count (<= 16), step count
+ * and dt, one precision (fp64 = 1: complex128, else complex64) and one
+ * quadrature (NONE, MIDPOINT or SIMPSON; no Magnus terms).  H0s[i] is dim x dim
+ * and H1s[i] holds amps[i] matrices back to back, as for setHamiltonian.
+ * Create uploads the Hamiltonians, plans the work and captures the persistent
+ * launch in a CUDA graph; SetSamples copies carrs[i] (amps[i] x pts[i]) to the
+ * device; Run replays the graph and copies each propagator to outs[i] (NULL:
+ * leave on the device); Tune times candidate work granularities on this
+ * ensemble and keeps the fastest.  Each problem uses the reference's scheme
+ * (norm bound, order table of the precision, Clenshaw, time-ordered product). */
+typedef struct Parament_Ensemble Parament_Ensemble;
+PARAMENT_API Parament_ErrorCode Parament_ensembleCreate(Parament_Ensemble **out, int fp64, unsigned int nprob,
+                                                        const unsigned int *dims, const unsigned int *amps,
+                                                        const unsigned int *pts, const double *dts,
+                                                        const void *const *H0s, const void *const *H1s,
+                                                        int quadrature);
+PARAMENT_API Parament_ErrorCode Parament_ensembleSetSamples(Parament_Ensemble *ens, const void *const *carrs);
+PARAMENT_API Parament_ErrorCode Parament_ensembleRun(Parament_Ensemble *ens, void *const *outs);
+PARAMENT_API Parament_ErrorCode Parament_ensembleTune(Parament_Ensemble *ens);
+PARAMENT_API double Parament_ensembleGranularity(Parament_Ensemble *ens);
+/* Device time of the last Run (graph launch to completion), milliseconds. */
+PARAMENT_API float Parament_ensembleLastMs(Parament_Ensemble *ens);
+PARAMENT_API Parament_ErrorCode Parament_ensembleDestroy(Parament_Ensemble *ens);
+
 /* equiprop that allocates no device memory (no counterpart in the reference).
  * For callers that must not call cudaMalloc while they propagate: real-time
  * loops that cannot wait on the allocator, applications whose device memory

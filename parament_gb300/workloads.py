@@ -83,3 +83,26 @@ def haar_unitary(d: int, seed: int = 1) -> np.ndarray:
     q, r = np.linalg.qr(z)
     ph = np.diag(r) / np.abs(np.diag(r))
     return q * ph[None, :]
+
+
+def ensemble(nprob=4096, seed=3, dt=1e-3):
+    """Batched workload: nprob problems with d in {4, 8, 16, 32, 64}
+    (probabilities .3/.3/.2/.15/.05), pts ~ U[256, 8192], K ~ U{1..4}.  Each
+    problem: H0 random Hermitian of norm 1 plus delta * Z_total with
+    delta ~ N(0, 0.05) and Z_total = sum_q Z_q over the log2(d) qubits
+    (diagonal entries sum_q (1 - 2 bit_q(i))); H_k random Hermitian of norm 1;
+    sinusoid-plus-noise controls.  Returns a list of (H0, H1, dt, carr)."""
+    rng = np.random.default_rng(seed)
+    dims = rng.choice([4, 8, 16, 32, 64], size=nprob, p=[0.3, 0.3, 0.2, 0.15, 0.05])
+    out = []
+    for d in dims:
+        d = int(d)
+        pts = int(rng.integers(256, 8193))
+        K = int(rng.integers(1, 5))
+        q = int(np.log2(d))
+        z = np.array([sum(1 - 2 * ((i >> b) & 1) for b in range(q)) for i in range(d)], dtype=float)
+        H0 = hermitian(rng, d, 1.0) + rng.normal(0.0, 0.05) * np.diag(z)
+        H1 = np.stack([hermitian(rng, d, 1.0) for _ in range(K)])
+        carr = sinusoid_controls(rng, K, pts, dt)
+        out.append((H0, H1, dt, carr))
+    return out
