@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--steps-per-prop", type=int, default=65536, help="time steps of the workload")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--forms", default="plain_c128,plain_c64,split_c64",
                    help="comma-separated forms to measure (plain_c128 is the error reference)")
     return p.parse_args()
@@ -277,6 +278,56 @@ def grape_block(torch, parament, K_steps, W_steps, flush, stream):
     return out
 
 
+def ensemble_block(torch, parament, K_steps, W_steps):
+    """Batched workload: 4096 complex64 problems of uneven d, steps and K in one
+    graph-captured persistent launch (autotuned), against one equiprop launch
+    per problem on pre-loaded contexts with device-resident samples."""
+    from parament_gb300 import workloads
+    from parament_gb300.ensemble import Ensemble
+    probs = workloads.ensemble()
+    steps = sum(c.shape[1] for *_, c in probs)
+    out = {"workload": "4096 problems, d in {4,8,16,32,64}, pts U[256,8192], K U{1..4}, complex64, NONE",
+           "total_steps": int(steps)}
+    ens = Ensemble([(H0, H1, dt, c.shape[1]) for H0, H1, dt, c in probs], "fp32")
+    ens.set_samples([c for *_, c in probs])
+    out["autotuned_granularity"] = ens.tune()
+    for _ in range(W_steps):
+        ens.run(copy_out=False)
+    ms = []
+    for _ in range(K_steps):
+        ens.run(copy_out=False)
+        ms.append(ens.last_ms)
+    t = sum(ms) / len(ms)
+    out["ensemble_ms"] = round(t, 3)
+    out["ensemble_steps_per_s"] = round(steps / (t * 1e-3), 1)
+    ens.destroy()
+    ctxs, carrs = [], []
+    for H0, H1, dt, c in probs:
+        cx = parament.Parament("fp32")
+        cx.set_hamiltonian(H0, *H1)
+        ctxs.append(cx)
+        carrs.append(torch.tensor(c, dtype=torch.complex64, device="cuda"))
+    outs = [torch.empty((H0.shape[0],) * 2, dtype=torch.complex64, device="cuda") for H0, *_ in probs]
+    stream = torch.cuda.current_stream()
+    for cx, c, o, (H0, H1, dt, _) in zip(ctxs, carrs, outs, probs):
+        cx.equiprop_device(dt, c, o, stream)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    s.record()
+    for cx, c, o, (H0, H1, dt, _) in zip(ctxs, carrs, outs, probs):
+        cx.equiprop_device(dt, c, o, stream)
+    e.record()
+    e.synchronize()
+    wall = time.perf_counter() - t0
+    out["per_problem_launch_ms"] = round(s.elapsed_time(e), 3)
+    out["per_problem_launch_wall_ms"] = round(wall * 1e3, 3)
+    out["speedup_vs_per_problem"] = round(s.elapsed_time(e) / t, 2)
+    for cx in ctxs:
+        cx.destroy()
+    return out
+
+
 def cpu_baseline(w, target_s=10.0):
     """The C restatement of the reference algorithm (oracle) on all host
     threads, over a bounded prefix of the workload's steps."""
@@ -461,6 +512,11 @@ def run_ours(args, rank, world, local):
         line["grape"] = grape_block(torch, parament, args.steps, args.warmup, flush, stream)
     except (ValueError, RuntimeError) as e:
         line["grape"] = {"error": str(e)}
+    if not args.no_ensemble:
+        try:
+            line["ensemble"] = ensemble_block(torch, parament, args.steps, args.warmup)
+        except (ValueError, RuntimeError, MemoryError) as e:
+            line["ensemble"] = {"error": str(e)}
     if not args.no_cpu_baseline:
         base, S, t = cpu_baseline(w)
         line["cpu_baseline"] = base
