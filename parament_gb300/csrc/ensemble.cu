@@ -206,8 +206,9 @@ __device__ __forceinline__ size_t ens_group_elems(int D) {
     return 3 * (size_t)D * (D + 1) + kEnsMaxK;
 }
 
+// Complex64 keeps to 128 registers so two CTAs (16 warps) share an SM.
 template <class R>
-__global__ void __launch_bounds__(256) k_ensemble(const __grid_constant__ EnsArgs<R> a) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_ensemble(const __grid_constant__ EnsArgs<R> a) {
     using C = cplx_t<R>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
@@ -319,9 +320,12 @@ static size_t ens_smem(bool fp64, int cls) {
     return es * (size_t)kClassGroups[cls] * (3 * (size_t)D * (D + 1) + kEnsMaxK);
 }
 
-// Cost of one step of a problem in "thread-MAC" units per CTA: products per
-// step times d^3 complex multiply-adds, spread over the CTA's 256 threads.
-static double step_cost(const EnsProblem &p) { return (double)p.M * p.d * p.d * p.d / 256.0; }
+// Time model of one step of a chunk: products per step times d^3 complex
+// multiply-adds over the CTA's 256 threads, plus a fixed part of about one
+// 32^3 product for the dependent load/synchronise chain every step pays
+// (weights, assembly, barriers) -- for d <= 16 that latency, not the
+// arithmetic, sets the step time, so small problems are cut into more chunks.
+static double step_cost(const EnsProblem &p) { return (double)p.M * ((double)p.d * p.d * p.d + 32768.0) / 256.0; }
 
 // Work list for a given granularity: chunk lengths chosen so that each
 // bundle costs about total / (slots * granularity).
@@ -604,7 +608,7 @@ Parament_ErrorCode Parament_ensembleTune(Parament_Ensemble *ens) {
     Ensemble *E = reinterpret_cast<Ensemble *>(ens);
     if (!E) return PARAMENT_STATUS_INVALID_VALUE;
     cudaSetDevice(E->device);
-    static const double cands[] = {1.0, 2.0, 4.0, 8.0, 16.0};
+    static const double cands[] = {1.0, 2.0, 4.0, 8.0, 16.0, 32.0, 64.0};
     double best_g = E->granularity;
     float best = 1e30f;
     for (double g : cands) {

@@ -75,7 +75,7 @@ def test_ensemble_tune_keeps_results(built_lib):
         ens.set_samples([c for *_, c in probs])
         before = ens.run()
         g = ens.tune()
-        assert g in (1.0, 2.0, 4.0, 8.0, 16.0)
+        assert g in (1.0, 2.0, 4.0, 8.0, 16.0, 32.0, 64.0)
         after = ens.run()
         assert ens.last_ms > 0
     for a, b in zip(before, after):
