@@ -28,6 +28,7 @@
 namespace pgb {
 
 constexpr int kEnsMaxK = 16;
+constexpr int kEnsRegK = 4;  // controls whose matrices a thread caches in registers
 constexpr int kEnsClasses = 5;
 static const int kClassDim[kEnsClasses] = {4, 8, 16, 32, 64};
 static const int kClassGroups[kEnsClasses] = {16, 4, 1, 1, 1};
@@ -87,8 +88,33 @@ __device__ void ens_chunk(const EnsArgs<R> &a, const EnsProblem &p, const EnsIte
     WeightSpec w{p.pts, p.K, p.K, p.mode, 0, 0.0};
     const C *carr = a.carr + p.carr_off;
     C b2[TM][TM], acc[TM][TM];
+    // The expansion matrices do not change from step to step: for TM <= 2 and
+    // up to kEnsRegK controls each thread keeps its own elements of them in
+    // registers for the whole chunk instead of re-reading them every step.
+    constexpr bool kCache = TM <= 2;
+    C hreg[kCache ? TM : 1][kCache ? TM : 1][kCache ? kEnsRegK + 1 : 1];
+    const bool cached = kCache && p.K <= kEnsRegK;
+    if (kCache && cached) {
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j) {
+                const int r = min(ty + T * i, d - 1), c = min(tx + T * j, d - 1);
+#pragma unroll
+                for (int m = 0; m <= kEnsRegK; ++m)
+                    hreg[kCache ? i : 0][kCache ? j : 0][kCache ? m : 0] =
+                        (m <= p.K) ? stack[(size_t)m * dd + r * d + c] : mk<C>(0.0, 0.0);
+            }
+    }
+    // Weight of the thread's control for the first step; later steps are
+    // fetched one step ahead so the sample load overlaps the step's products.
+    C wnext = (gt < p.K) ? step_weight(carr, w, gt, it.s0) : mk<C>(0.0, 0.0);
     for (long long st = it.s0; st < it.s1; ++st) {
-        for (int m = gt; m < p.K; m += T * T) ws[m] = step_weight(carr, w, m, st);
+        if (gt < p.K) {
+            ws[gt] = wnext;
+            if (st + 1 < it.s1) wnext = step_weight(carr, w, gt, st + 1);
+        }
+        for (int m = gt + T * T; m < p.K; m += T * T) ws[m] = step_weight(carr, w, m, st);
         group_sync<D>(g);
 #pragma unroll
         for (int i = 0; i < TM; ++i)
@@ -96,8 +122,16 @@ __device__ void ens_chunk(const EnsArgs<R> &a, const EnsProblem &p, const EnsIte
             for (int j = 0; j < TM; ++j) {
                 const int r = ty + T * i, c = tx + T * j;
                 if (r >= d || c >= d) continue;
-                C v = stack[r * d + c];
-                for (int m = 0; m < p.K; ++m) cfma(v, ws[m], stack[(size_t)(m + 1) * dd + r * d + c]);
+                C v;
+                if (kCache && cached) {
+                    v = hreg[kCache ? i : 0][kCache ? j : 0][0];
+#pragma unroll
+                    for (int m = 0; m < kEnsRegK; ++m)
+                        if (m < p.K) cfma(v, ws[m], hreg[kCache ? i : 0][kCache ? j : 0][kCache ? m + 1 : 0]);
+                } else {
+                    v = stack[r * d + c];
+                    for (int m = 0; m < p.K; ++m) cfma(v, ws[m], stack[(size_t)(m + 1) * dd + r * d + c]);
+                }
                 Xs[r * ld + c] = v;
                 C bm1 = cscale(cmul(J[M], v), s);
                 if (r == c) bm1 = cadd(bm1, J[M - 1]);
@@ -206,52 +240,28 @@ __device__ __forceinline__ size_t ens_group_elems(int D) {
     return 3 * (size_t)D * (D + 1) + kEnsMaxK;
 }
 
-// Complex64 keeps to 128 registers so two CTAs (16 warps) share an SM.
-template <class R>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_ensemble(const __grid_constant__ EnsArgs<R> a) {
+// One persistent kernel per dimension class, so each gets its own register
+// budget and occupancy: CTAs pull bundles of that class from the class's
+// counter until the class is exhausted.
+template <class R, int TM, int D, int GROUPS, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_ensemble_class(const __grid_constant__ EnsArgs<R> a, int first,
+                                                              int count, int *counter) {
     using C = cplx_t<R>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
+    constexpr int GT = 256 / GROUPS;  // threads per group
     __shared__ int bid;
     for (;;) {
-        if (threadIdx.x == 0) bid = atomicAdd(a.counter, 1);
+        if (threadIdx.x == 0) bid = atomicAdd(counter, 1);
         __syncthreads();
         const int b = bid;
         __syncthreads();
-        if (b >= a.nbundles) break;
-        const EnsBundle B = a.bundles[b];
-        switch (B.cls) {
-            case 0: {
-                const int g = threadIdx.x / 16, gt = threadIdx.x % 16;
-                if (g < B.count) {
-                    const EnsItem it = a.items[B.first + g];
-                    ens_chunk<R, 1, 4>(a, a.probs[it.prob], it, g, gt, sm + g * ens_group_elems<R>(4));
-                }
-                break;
-            }
-            case 1: {
-                const int g = threadIdx.x / 64, gt = threadIdx.x % 64;
-                if (g < B.count) {
-                    const EnsItem it = a.items[B.first + g];
-                    ens_chunk<R, 1, 8>(a, a.probs[it.prob], it, g, gt, sm + g * ens_group_elems<R>(8));
-                }
-                break;
-            }
-            case 2: {
-                const EnsItem it = a.items[B.first];
-                ens_chunk<R, 1, 16>(a, a.probs[it.prob], it, 0, threadIdx.x, sm);
-                break;
-            }
-            case 3: {
-                const EnsItem it = a.items[B.first];
-                ens_chunk<R, 2, 32>(a, a.probs[it.prob], it, 0, threadIdx.x, sm);
-                break;
-            }
-            default: {
-                const EnsItem it = a.items[B.first];
-                ens_chunk<R, 4, 64>(a, a.probs[it.prob], it, 0, threadIdx.x, sm);
-                break;
-            }
+        if (b >= count) break;
+        const EnsBundle B = a.bundles[first + b];
+        const int g = threadIdx.x / GT, gt = threadIdx.x % GT;
+        if (g < B.count) {
+            const EnsItem it = a.items[B.first + g];
+            ens_chunk<R, TM, D>(a, a.probs[it.prob], it, g, gt, sm + g * ens_group_elems<R>(D));
         }
         __syncthreads();
     }
@@ -300,11 +310,12 @@ struct Ensemble {
     DevBuf d_probs, d_items, d_bundles, d_counter, d_stack, d_carr, d_J, d_chunks, d_out;
     void *h_carr = nullptr, *h_out = nullptr;  // pinned staging
     int nbundles = 0;
+    int cls_first[kEnsClasses] = {0}, cls_count[kEnsClasses] = {0};
+    int cls_slots[kEnsClasses] = {0};
     double granularity = 4.0;  // bundles per resident CTA (autotuned)
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_ms = -1.0f;
-    size_t smem = 0;
     int slots = 0;
 };
 
@@ -332,7 +343,7 @@ static double step_cost(const EnsProblem &p) { return (double)p.M * ((double)p.d
 static Parament_ErrorCode build_work(Ensemble *E, double gran) {
     double total = 0.0;
     for (auto &p : E->probs) total += step_cost(p) * p.P / kClassGroups[class_of(p.d)];
-    const double target = std::max(1.0, total / (E->slots * gran));
+    const double target = std::max(1.0, total / (E->slots * gran));  // slots: CTAs of the d=64 class
     std::vector<EnsItem> items;
     std::vector<EnsBundle> bundles;
     long long chunk_elems = 0;
@@ -350,11 +361,13 @@ static Parament_ErrorCode build_work(Ensemble *E, double gran) {
     // Largest classes first so the long bundles start early.
     for (int c = kEnsClasses - 1; c >= 0; --c) {
         auto &v = per_class[c];
+        E->cls_first[c] = (int)bundles.size();
         for (size_t k = 0; k < v.size(); k += kClassGroups[c]) {
             const int cnt = (int)std::min<size_t>(kClassGroups[c], v.size() - k);
             bundles.push_back(EnsBundle{c, cnt, (int)items.size()});
             for (int q = 0; q < cnt; ++q) items.push_back(v[k + q]);
         }
+        E->cls_count[c] = (int)bundles.size() - E->cls_first[c];
     }
     const size_t es = E->fp64 ? 16 : 8;
     if (E->d_probs.ensure(sizeof(EnsProblem) * E->probs.size()) != cudaSuccess ||
@@ -374,10 +387,31 @@ static Parament_ErrorCode build_work(Ensemble *E, double gran) {
     return PARAMENT_STATUS_SUCCESS;
 }
 
+template <class R, int TM, int D, int GROUPS, int MINB>
+static cudaError_t launch_class(Ensemble *E, const EnsArgs<R> &a, int c) {
+    if (E->cls_count[c] == 0) return cudaSuccess;
+    const int grid = std::max(1, std::min(E->cls_slots[c], E->cls_count[c]));
+    int *counter = static_cast<int *>(E->d_counter.ptr) + c;
+    k_ensemble_class<R, TM, D, GROUPS, MINB><<<grid, 256, ens_smem(E->fp64, c), E->stream>>>(
+        a, E->cls_first[c], E->cls_count[c], counter);
+    return cudaGetLastError();
+}
+
+template <class R>
+static const void *class_kernel(int c) {
+    switch (c) {
+        case 0: return reinterpret_cast<const void *>(&k_ensemble_class<R, 1, 4, 16, 4>);
+        case 1: return reinterpret_cast<const void *>(&k_ensemble_class<R, 1, 8, 4, 4>);
+        case 2: return reinterpret_cast<const void *>(&k_ensemble_class<R, 1, 16, 1, 4>);
+        case 3: return reinterpret_cast<const void *>(&k_ensemble_class<R, 2, 32, 1, sizeof(R) == 4 ? 3 : 2>);
+        default: return reinterpret_cast<const void *>(&k_ensemble_class<R, 4, 64, 1, sizeof(R) == 4 ? 2 : 1>);
+    }
+}
+
 template <class R>
 static cudaError_t enqueue_t(Ensemble *E) {
     using C = cplx_t<R>;
-    cudaError_t e = cudaMemsetAsync(E->d_counter.ptr, 0, sizeof(int), E->stream);
+    cudaError_t e = cudaMemsetAsync(E->d_counter.ptr, 0, sizeof(int) * kEnsClasses, E->stream);
     if (e != cudaSuccess) return e;
     EnsArgs<R> a;
     a.probs = static_cast<const EnsProblem *>(E->d_probs.ptr);
@@ -389,9 +423,12 @@ static cudaError_t enqueue_t(Ensemble *E) {
     a.carr = static_cast<const C *>(E->d_carr.ptr);
     a.J = static_cast<const C *>(E->d_J.ptr);
     a.chunks = static_cast<C *>(E->d_chunks.ptr);
-    const int grid = std::max(1, std::min(E->slots, E->nbundles));
-    k_ensemble<R><<<grid, 256, E->smem, E->stream>>>(a);
-    e = cudaGetLastError();
+    // Largest dimension first: its bundles are the longest.
+    e = launch_class<R, 4, 64, 1, sizeof(R) == 4 ? 2 : 1>(E, a, 4);
+    if (e == cudaSuccess) e = launch_class<R, 2, 32, 1, sizeof(R) == 4 ? 3 : 2>(E, a, 3);
+    if (e == cudaSuccess) e = launch_class<R, 1, 16, 1, 4>(E, a, 2);
+    if (e == cudaSuccess) e = launch_class<R, 1, 8, 4, 4>(E, a, 1);
+    if (e == cudaSuccess) e = launch_class<R, 1, 4, 16, 4>(E, a, 0);
     if (e != cudaSuccess) return e;
     const size_t rsmem = 2 * sizeof(C) * 64 * 65;
     k_ensemble_reduce<R><<<(int)E->probs.size(), 256, rsmem, E->stream>>>(
@@ -428,16 +465,17 @@ static float timed_run(Ensemble *E) {
 
 template <class R>
 static void set_kernel_smem(Ensemble *E) {
-    size_t m = 0;
-    for (int c = 0; c < kEnsClasses; ++c) m = std::max(m, ens_smem(E->fp64, c));
-    E->smem = m;
-    cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_ensemble<R>), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)m);
+    for (int c = 0; c < kEnsClasses; ++c) {
+        const void *fn = class_kernel<R>(c);
+        const size_t m = ens_smem(E->fp64, c);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m);
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, m);
+        E->cls_slots[c] = std::max(1, per_sm) * E->num_sms;
+    }
     cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_ensemble_reduce<R>),
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(2 * sizeof(cplx_t<R>) * 64 * 65));
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void *>(&k_ensemble<R>), 256, m);
-    E->slots = std::max(1, per_sm) * E->num_sms;
+    E->slots = E->cls_slots[4];
 }
 
 }  // namespace pgb
@@ -514,7 +552,7 @@ Parament_ErrorCode Parament_ensembleCreate(Parament_Ensemble **out, int fp64, un
     if (r == PARAMENT_STATUS_SUCCESS) {
         if (E->d_stack.ensure(es * stack_elems) != cudaSuccess || E->d_carr.ensure(es * std::max(1LL, carr_elems)) != cudaSuccess ||
             E->d_J.ensure(es * (J.size() / 2)) != cudaSuccess || E->d_out.ensure(es * out_elems) != cudaSuccess ||
-            E->d_counter.ensure(sizeof(int)) != cudaSuccess ||
+            E->d_counter.ensure(sizeof(int) * kEnsClasses) != cudaSuccess ||
             cudaMallocHost(&E->h_carr, es * std::max(1LL, carr_elems)) != cudaSuccess ||
             cudaMallocHost(&E->h_out, es * out_elems) != cudaSuccess)
             r = PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
