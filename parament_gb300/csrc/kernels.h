@@ -68,6 +68,13 @@ struct GemmLaunch {
 };
 cudaError_t launch_gemm(const GemmLaunch &g);
 
+// tcgen05 tensor-core complex64 GEMM (3xTF32), used by launch_gemm for
+// complex64 with d >= 256 and d % 128 == 0.  tc_take_faults returns (and
+// clears) the number of CTAs whose bounded waits gave up.
+bool tc_gemm_applies(const GemmLaunch &g);
+cudaError_t launch_tc_gemm(const GemmLaunch &g);
+int tc_take_faults();
+
 // Ordered product of n d x d matrices (later index on the left), pairwise tree
 // as src/cuda/parament.cpp:677-714.  `work` holds n*d*d elements and may be
 // overwritten; `in` is overwritten too.  The result is copied into `out`.

@@ -368,6 +368,8 @@ static Parament_ErrorCode equiprop_host(Ctx *c, const void *carr, double dt, uns
         cudaGetLastError();
         return c->last_error = PARAMENT_STATUS_CUBLAS_FAILED;
     }
+    if (!c->fp64 && c->dim > (unsigned)kSmallMaxDim && tc_take_faults() > 0)
+        return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
     return c->last_error = PARAMENT_STATUS_SUCCESS;
 }
 
