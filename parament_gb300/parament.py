@@ -46,6 +46,16 @@ _EXCEPTIONS = {
     PARAMENT_STATUS_KERNEL_TIMEOUT: RuntimeError,
 }
 
+# Handle of CUDA's legacy default stream.  torch reports its default stream as
+# handle 0, which the C-ABI reads as "the context's own stream"; passing the
+# legacy handle keeps the work on the caller's stream.
+_CUDA_STREAM_LEGACY = 1
+
+
+def _stream_handle(stream):
+    return ctypes.c_void_p(stream.cuda_stream or _CUDA_STREAM_LEGACY)
+
+
 _QUADRATURE = {
     'none': PARAMENT_QUADRATURE_NONE,
     'midpoint': PARAMENT_QUADRATURE_MIDPOINT,
@@ -251,8 +261,7 @@ class Parament:
         if stream is None:
             stream = torch.cuda.current_stream(carr.device)
         code = self._fn('Parament_equipropDevice')(self._handle, ctypes.c_void_p(carr.data_ptr()), float(dt), pts,
-                                                   amps, ctypes.c_void_p(out.data_ptr()),
-                                                   ctypes.c_void_p(stream.cuda_stream))
+                                                   amps, ctypes.c_void_p(out.data_ptr()), _stream_handle(stream))
         self._check_error(code)
         return out
 
@@ -311,8 +320,7 @@ class Parament:
             stream = torch.cuda.current_stream(carr.device)
         code = self._fn('Parament_equipropVJPDevice')(self._handle, ctypes.c_void_p(carr.data_ptr()), float(dt),
                                                       pts, amps, ctypes.c_void_p(W.data_ptr()),
-                                                      ctypes.c_void_p(grad.data_ptr()),
-                                                      ctypes.c_void_p(stream.cuda_stream))
+                                                      ctypes.c_void_p(grad.data_ptr()), _stream_handle(stream))
         self._check_error(code)
         return grad
 
