@@ -80,6 +80,22 @@ __global__ void __launch_bounds__(256, 1) k_tc_cgemm(const __grid_constant__ TcA
         const float2 *A = g.A + (size_t)b * g.sA;
         const float2 *B = g.B + (size_t)b * g.sB;
         const int nk = d / 16;
+        // Slab kc + 1 is loaded into registers while slab kc is converted and
+        // multiplied, so global latency overlaps the tensor-core work.
+        float2 ra[8], rb[4];
+        auto load_slab = [&](int kc) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int e = tid + 256 * i, row = e >> 4, kk = e & 15;
+                ra[i] = A[(size_t)(r0 + row) * d + 16 * kc + kk];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int e = tid + 256 * i, kk = e >> 6, nn = e & 63;
+                rb[i] = B[(size_t)(16 * kc + kk) * d + c0 + nn];
+            }
+        };
+        load_slab(0);
         for (int kc = 0; kc < nk; ++kc) {
             const int s = kc & 1;
             unsigned char *Ah = smem + s * kTcStageBytes, *Al = Ah + kTcTileBytes;
@@ -89,25 +105,25 @@ __global__ void __launch_bounds__(256, 1) k_tc_cgemm(const __grid_constant__ TcA
                 if (!tc::mbar_wait(&mbar[s], (issued[s] - 1) & 1, kTcWaitLimit)) ok = false;
             }
             // A' slab: rows r0..r0+127, complex columns 16 kc .. 16 kc + 15.
-#pragma unroll 4
+#pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const int e = tid + 256 * i, row = e >> 4, kk = e & 15;
-                const int gk = 16 * kc + kk;
-                float2 a = A[(size_t)(r0 + row) * d + gk];
-                if (g.a_minus_identity && r0 + row == gk) a.x -= 1.0f;
+                float2 a = ra[i];
+                if (g.a_minus_identity && r0 + row == 16 * kc + kk) a.x -= 1.0f;
                 put_split(Ah, Al, tc::sw128_offset(row, kk), a.x);
                 put_split(Ah, Al, tc::sw128_offset(row, 16 + kk), a.y);
             }
             // B''^T slab: rows n (0..63: real part of C, 64..127: imaginary), K = 32.
-#pragma unroll 4
+#pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const int e = tid + 256 * i, kk = e >> 6, nn = e & 63;
-                const float2 v = B[(size_t)(16 * kc + kk) * d + c0 + nn];
+                const float2 v = rb[i];
                 put_split(Bh, Bl, tc::sw128_offset(nn, kk), v.x);
                 put_split(Bh, Bl, tc::sw128_offset(nn, 16 + kk), -v.y);
                 put_split(Bh, Bl, tc::sw128_offset(64 + nn, kk), v.y);
                 put_split(Bh, Bl, tc::sw128_offset(64 + nn, 16 + kk), v.x);
             }
+            if (kc + 1 < nk) load_slab(kc + 1);
             tc::fence_proxy_async();
             __syncthreads();
             if (tid == 0) {
