@@ -328,6 +328,38 @@ def ensemble_block(torch, parament, K_steps, W_steps):
     return out
 
 
+def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, steps=1024):
+    """Large dense workload, complex64 d=512, K=8, ||H0|| = 20, smooth
+    8-mode Fourier controls, on a 1024-step prefix of the 8192 steps: the
+    tcgen05 3xTF32 GEMM path (kernel k_tc_cgemm)."""
+    from parament_gb300 import workloads
+    w = workloads.large_dense(d=512, K=8, steps=steps)
+    ctx = parament.Parament("fp32")
+    ctx.set_hamiltonian(w["H0"], *w["H1"])
+    carr = torch.tensor(w["carr"], dtype=torch.complex64, device="cuda")
+    out = torch.empty((512, 512), dtype=torch.complex64, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(W_steps):
+            ctx.equiprop_device(w["dt"], carr, out, stream)
+        stream.synchronize()
+        ts = []
+        for _ in range(K_steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            ctx.equiprop_device(w["dt"], carr, out, stream)
+            e.record(stream)
+            ts.append((s, e))
+        stream.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ts) / len(ts)
+    M = ctx.last_iteration_cycles
+    ctx.destroy()
+    flops = steps * (M + 1) * 8.0 * 512 ** 3
+    return {"workload": f"large_dense d=512 K=8 complex64, first {steps} steps", "M": M, "ms": round(ms, 3),
+            "steps_per_s": round(steps / (ms * 1e-3), 1), "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
+            "kernel": "k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)"}
+
+
 def cpu_baseline(w, target_s=10.0):
     """The C restatement of the reference algorithm (oracle) on all host
     threads, over a bounded prefix of the workload's steps."""
@@ -512,6 +544,10 @@ def run_ours(args, rank, world, local):
         line["grape"] = grape_block(torch, parament, args.steps, args.warmup, flush, stream)
     except (ValueError, RuntimeError) as e:
         line["grape"] = {"error": str(e)}
+    try:
+        line["large_dense"] = large_dense_block(torch, parament, args.steps, args.warmup, flush, stream)
+    except (ValueError, RuntimeError) as e:
+        line["large_dense"] = {"error": str(e)}
     if not args.no_ensemble:
         try:
             line["ensemble"] = ensemble_block(torch, parament, args.steps, args.warmup)

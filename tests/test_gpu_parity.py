@@ -195,3 +195,38 @@ def test_device_allocation_failure_is_reported(built_lib):
     env = dict(os.environ, PARAMENT_FAIL_ALLOC_AFTER="2")
     r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
     assert "MEMERR Error code 20" in r.stdout, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("d,P", [(256, 6), (384, 3)])
+def test_tensor_core_large_dimension(built_lib, d, P):
+    """complex64, d >= 256: the tcgen05 3xTF32 GEMM path against the oracle."""
+    rng = np.random.default_rng(d + P)
+    from parament_gb300.workloads import hermitian
+    H0 = hermitian(rng, d, 5.0)
+    H1 = np.stack([hermitian(rng, d, 1.0) for _ in range(2)])
+    carr = rng.standard_normal((2, P))
+    U, M = run(H0, H1, list(carr), 2e-3, precision="fp32")
+    H0, H1, carr = (x.astype(np.complex64).astype(np.complex128) for x in (H0, H1, carr))
+    Uo, Mo, _, _ = oracle.equiprop(H0, H1, carr, 2e-3, single=True, nthreads=os.cpu_count())
+    assert M == Mo
+    assert relerr(U, Uo) < TOL["fp32"]
+
+
+def test_tensor_core_matches_simt_gemm(built_lib):
+    """d=512: the tcgen05 path and the SIMT GEMM path (tensor cores disabled
+    through PARAMENT_DISABLE_TENSOR_CORES in a child process) agree."""
+    code = ("import sys, numpy as np, parament_gb300 as p\n"
+            "from parament_gb300 import workloads\n"
+            "w = workloads.large_dense(d=512, K=8, steps=5)\n"
+            "c = p.Parament('fp32'); c.set_hamiltonian(w['H0'], *w['H1'])\n"
+            "np.save(sys.argv[1], c.equiprop(w['dt'], *w['carr']))\n")
+    import tempfile
+    outs = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for tag, env in (("tc", {}), ("simt", {"PARAMENT_DISABLE_TENSOR_CORES": "1"})):
+            f = os.path.join(tmp, tag + ".npy")
+            r = subprocess.run([sys.executable, "-c", code, f], cwd=ROOT, env=dict(os.environ, **env),
+                               capture_output=True, text=True, timeout=600)
+            assert r.returncode == 0, r.stderr
+            outs.append(np.load(f).astype(np.complex128))
+    assert relerr(outs[0], outs[1]) < 1e-5
