@@ -44,7 +44,7 @@ struct Ctx {
 
     // Precision form (complex64 contexts)
     int precision = PARAMENT_PRECISION_PLAIN;
-    DevBuf split_stack;                          // double-float copy of the stack
+    DevBuf split_stack;                          // split form's stack (commutators from FP64)
     bool split_ready = false;
 
     // Instrumentation: CUDA events around the dominant kernel of the last call

@@ -12,7 +12,8 @@
 // with mu_n = m_n / Hnorm^n and m_n the monomial coefficients of
 // J_0 + 2 sum_k (-i)^k J_k(x) T_k(t).  The first- and second-order terms
 // (|mu_1 X| ~ Hnorm dt, |mu_2 X^2| ~ (Hnorm dt)^2) are formed in double-float
-// (pairs of floats) from a double-float copy of the expansion stack; X^2 uses
+// (pairs of floats), X itself accumulated in double-float from FP64 weights
+// and the complex64 expansion stack; X^2 uses
 // the three products hi*hi + hi*lo + lo*hi; the higher orders, whose size is
 // below 1e-5 of the result, stay in FP32.  Each CTA multiplies its chunk of
 // consecutive steps into E^P (P = I + E^P) held in double-float, adding the
@@ -102,7 +103,7 @@ __device__ __forceinline__ float2 cdf_lo(cdf a) { return make_float2(a.re.lo, a.
 struct SplitArgs {
     double2 c0;                         // m_0 - 1
     double2 mu[kSplitMaxOrder + 1];     // mu_n, n = 1..M
-    const float4 *stack;                // (1+Ke) matrices: (re_hi, im_hi, re_lo, im_lo)
+    const float2 *stack;                // (1+Ke) complex64 matrices (commutators rounded from FP64)
     const float2 *carr;                 // samples (complex64)
     double2 *chunks;                    // nchunks products I + E^P, complex128
     long long P;
@@ -232,38 +233,62 @@ __global__ void __launch_bounds__(256, 1) k_split_steps(const __grid_constant__ 
         }
         __syncthreads();
         // X = H0 + sum_m w_m H_m in double-float; E starts as (m_0-1) I + mu_1 X.
+        // X = H0 + sum_m w_m H_m.  The matrices are complex64 (H0 and H_k are
+        // the caller's complex64 inputs, exact; the Magnus commutators are
+        // formed in FP64 and rounded).  Control slots (< K) carry FP64 weights
+        // as float pairs and accumulate in double-float; the commutator slots
+        // carry weights of order dt |du| and accumulate in FP32 -- their
+        // rounding is far below the error bar even when it repeats at every
+        // step.  The loop runs matrix by matrix so that a thread's loads of
+        // one matrix are independent and in flight together.
+        {
+            cdf xa[TM][TM];
+            float2 sa[TM][TM];
 #pragma unroll
-        for (int i = 0; i < TM; ++i)
+            for (int i = 0; i < TM; ++i)
 #pragma unroll
-            for (int j = 0; j < TM; ++j) {
-                if (!own[i][j]) continue;
-                const int e = eo[i][j];
-                const int ge = (ty + 16 * i) * d + tx + 16 * j;
-                // Controls (slots < K): FP64 weights as float pairs times
-                // matrices that are exact in float, accumulated in
-                // double-float.  Magnus commutator slots carry weights of
-                // order dt |du| and stay in FP32: their rounding is far below
-                // the error bar even when it repeats at every step.
-                float4 h = a.stack[ge];
-                cdf x = {{h.x, h.z}, {h.y, h.w}};
-                float2 small = make_float2(0.f, 0.f);
-                for (int m = 0; m < a.Ke; ++m) {
-                    float4 g = a.stack[(size_t)(m + 1) * dd + ge];
-                    float4 w = ws[m];
-                    if (m < a.K) {
-                        cdf wd = {{w.x, w.y}, {w.z, w.w}};
-                        x = cdf_add(x, cdf_mul(wd, cdf{{g.x, g.z}, {g.y, g.w}}));
-                    } else {
-                        cfma(small, make_float2(w.x, w.z), make_float2(g.x, g.y));
-                    }
+                for (int j = 0; j < TM; ++j) {
+                    float2 h = own[i][j] ? a.stack[(ty + 16 * i) * d + tx + 16 * j] : make_float2(0.f, 0.f);
+                    xa[i][j] = cdf{{h.x, 0.f}, {h.y, 0.f}};
+                    sa[i][j] = make_float2(0.f, 0.f);
                 }
-                x = cdf_add_c(x, small);
-                Xh[e] = cdf_hi(x);
-                Xl[e] = cdf_lo(x);
-                cdf v = cdf_mul(mu1, x);
-                if (dg[i][j]) v = cdf_add(v, c0);
-                E[i][j] = v;
+            for (int m = 0; m < a.Ke; ++m) {
+                const float2 *Hm = a.stack + (size_t)(m + 1) * dd;
+                const float4 w = ws[m];
+                float2 g[TM][TM];
+#pragma unroll
+                for (int i = 0; i < TM; ++i)
+#pragma unroll
+                    for (int j = 0; j < TM; ++j)
+                        g[i][j] = own[i][j] ? Hm[(ty + 16 * i) * d + tx + 16 * j] : make_float2(0.f, 0.f);
+                if (m < a.K) {
+                    const cdf wd = {{w.x, w.y}, {w.z, w.w}};
+#pragma unroll
+                    for (int i = 0; i < TM; ++i)
+#pragma unroll
+                        for (int j = 0; j < TM; ++j) xa[i][j] = cdf_add(xa[i][j], cdf_mul_c(wd, g[i][j]));
+                } else {
+                    const float2 wf = make_float2(w.x, w.z);
+#pragma unroll
+                    for (int i = 0; i < TM; ++i)
+#pragma unroll
+                        for (int j = 0; j < TM; ++j) cfma(sa[i][j], wf, g[i][j]);
+                }
             }
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) {
+                    if (!own[i][j]) continue;
+                    const int e = eo[i][j];
+                    const cdf x = cdf_add_c(xa[i][j], sa[i][j]);
+                    Xh[e] = cdf_hi(x);
+                    Xl[e] = cdf_lo(x);
+                    cdf v = cdf_mul(mu1, x);
+                    if (dg[i][j]) v = cdf_add(v, c0);
+                    E[i][j] = v;
+                }
+        }
         __syncthreads();
         // G2 = X^2 = Xh Xh + (Xh Xl + Xl Xh).
         tile_gemm_f<TM, false>(acc, Xh, Xh, nullptr, nullptr, d, ld, ty, tx);
@@ -372,13 +397,10 @@ __global__ void k_c128_to_c64(const double2 *src, float2 *dst, int n) {
     if (i < n) dst[i] = make_float2((float)src[i].x, (float)src[i].y);
 }
 
-// Double-float stack from the FP64 stack: (re_hi, im_hi, re_lo, im_lo).
-__global__ void k_split_stack(const double2 *src, float4 *dst, long long n) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double2 v = src[i];
-        float rh = (float)v.x, ih = (float)v.y;
-        dst[i] = make_float4(rh, ih, (float)(v.x - (double)rh), (float)(v.y - (double)ih));
-    }
+// Complex64 stack from the FP64 stack (round to nearest).
+__global__ void k_split_stack(const double2 *src, float2 *dst, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = make_float2((float)src[i].x, (float)src[i].y);
 }
 __global__ void k_c64_to_c128(const float2 *src, double2 *dst, long long n) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -449,13 +471,13 @@ static void split_coefficients(int M, double x, double hnorm, double *c0, std::v
     }
 }
 
-// Builds the double-float stack: the complex64 inputs promoted to FP64, the
-// Magnus commutators recomputed in FP64, split into float pairs.
+// Builds the split form's stack: the complex64 inputs (exact), and the Magnus
+// commutators recomputed in FP64 from them and rounded to complex64.
 static Parament_ErrorCode prepare_split_stack(Ctx *c) {
     if (c->split_ready) return PARAMENT_STATUS_SUCCESS;
     const size_t dd = (size_t)c->dim * c->dim, n = dd * (1 + c->Ke);
     DevBuf tmp;
-    if (tmp.ensure(n * sizeof(double2)) != cudaSuccess || c->split_stack.ensure(n * sizeof(float4)) != cudaSuccess) {
+    if (tmp.ensure(n * sizeof(double2)) != cudaSuccess || c->split_stack.ensure(n * sizeof(float2)) != cudaSuccess) {
         tmp.release();
         return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
     }
@@ -492,7 +514,7 @@ static Parament_ErrorCode prepare_split_stack(Ctx *c) {
                 e = commutator(1 + j, 1 + i, 1 + 2 * K + i * (i - 1) / 2 + j);
     }
     if (e == cudaSuccess) {
-        k_split_stack<<<512, 256, 0, c->stream>>>(s64, static_cast<float4 *>(c->split_stack.ptr), (long long)n);
+        k_split_stack<<<512, 256, 0, c->stream>>>(s64, static_cast<float2 *>(c->split_stack.ptr), (long long)n);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -519,7 +541,7 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
     a.c0 = make_double2(c0[0], c0[1]);
     for (int n = 0; n <= kSplitMaxOrder; ++n)
         a.mu[n] = (n >= 1 && n <= M) ? make_double2(mu[2 * n], mu[2 * n + 1]) : make_double2(0, 0);
-    a.stack = static_cast<const float4 *>(c->split_stack.ptr);
+    a.stack = static_cast<const float2 *>(c->split_stack.ptr);
     a.carr = static_cast<const float2 *>(d_carr);
     a.P = P;
     a.d = d;
