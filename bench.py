@@ -48,6 +48,9 @@ def parse():
     p.add_argument("--steps-per-prop", type=int, default=65536, help="time steps of the workload")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
+    p.add_argument("--profile-case", default=None,
+                   choices=["split_c64", "plain_c64", "plain_c128", "large_dense_d512", "vjp_d32"],
+                   help="run one form twice (for ncu captures) and exit")
     p.add_argument("--forms", default="plain_c128,plain_c64,split_c64",
                    help="comma-separated forms to measure (plain_c128 is the error reference)")
     return p.parse_args()
@@ -559,8 +562,45 @@ def run_ours(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def profile_case(args):
+    """Small fixed invocations for ncu: the named form, two calls, no timing."""
+    import torch
+
+    import parament_gb300 as parament
+    from parament_gb300 import workloads
+    case = args.profile_case
+    if case == "large_dense_d512":
+        w = workloads.large_dense(d=512, K=8, steps=32)
+        ctx = parament.Parament("fp32")
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+    elif case == "vjp_d32":
+        w = workloads.adjoint_d32(steps=args.steps_per_prop)
+        ctx = parament.Parament("fp32")
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+    else:
+        w = workloads.magnus_d64(args.steps_per_prop)
+        ctx = parament.Parament("fp64" if case == "plain_c128" else "fp32")
+        ctx.set_hamiltonian(w["H0"], *w["H1"], use_magnus=True, quadrature_mode="simpson")
+        if case == "split_c64":
+            ctx.set_precision_mode("split")
+    ct = torch.complex128 if case == "plain_c128" else torch.complex64
+    carr = torch.tensor(w["carr"], dtype=ct, device="cuda")
+    for _ in range(2):
+        if case == "vjp_d32":
+            W = torch.eye(32, dtype=ct, device="cuda")
+            ctx.vjp_device(w["dt"], carr, W)
+        else:
+            ctx.equiprop_device(w["dt"], carr)
+    torch.cuda.synchronize()
+    ctx.destroy()
+    print("profile case", case, "done")
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args)
+        return
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))
