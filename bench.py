@@ -513,7 +513,7 @@ def run_ours(args, rank, world, local):
     achieved = fl / (kms * 1e-3) / 1e12
     pipe_peak = lib_peaks["fp64_gemm_tflops"] if head == "plain_c128" else lib_peaks["fp32_gemm_tflops"]
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             traffic = json.load(f).get(head)
