@@ -75,6 +75,12 @@ bool tc_gemm_applies(const GemmLaunch &g);
 cudaError_t launch_tc_gemm(const GemmLaunch &g);
 int tc_take_faults();
 
+// Tensor-core form of the split complex64 kernel (d = 64): whether it serves
+// this problem, and the number (cleared on read) of CTAs whose bounded waits
+// on the tensor core gave up.
+bool split_tc_applies(int d, int Ke, int M);
+int split_tc_take_faults();
+
 // Ordered product of n d x d matrices (later index on the left), pairwise tree
 // as src/cuda/parament.cpp:677-714.  `work` holds n*d*d elements and may be
 // overwritten; `in` is overwritten too.  The result is copied into `out`.

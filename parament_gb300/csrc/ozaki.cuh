@@ -1,0 +1,151 @@
+// Sliced complex products with exact accumulation on the tcgen05 tensor cores.
+//
+// A product C = A B of two 64 x 64 complex matrices is computed from bf16
+// slices of integers: every row r of A is scaled by 2^(7 - ea_r) and every
+// column n of B by 2^(7 - eb_n) (ea, eb the exponents of the row / column
+// maxima), and the scaled values are peeled into slices
+//     t = sum_s q_s 2^(-8 s),   q_s integers in [-128, 128]
+// (round to nearest at every peel, so the truncation is unbiased).  Products
+// of slices are integers of at most 2^14; K = 128 of them sum to at most 2^21,
+// and the products of one level L = s + t (at most four) to at most 2^23, so
+// the FP32 accumulators in tensor memory hold every level exactly.  The
+// epilogue forms C = 2^(ea_r + eb_n - 14) sum_L 2^(-8 L) D_L.  With S slices
+// and levels up to S - 1, C is exact up to about 2^(-8 S) of the row / column
+// scales; S = 4 goes well beyond FP32, S = 2 is enough for small terms.
+//
+// Real formulation (M = 128 rows, N = 64 columns, K = 128):
+//     [C_r; C_i] = [[A_r, -A_i], [A_i, A_r]] [B_r; B_i]
+// The A operand of one slice is stored as three 64-row blocks [-A_i][A_r][A_i]
+// so that the first K half reads [A_r; A_i] and the second [-A_i; A_r] as one
+// contiguous 128-row operand each.  B is stored K-major as [B_r^T | B_i^T].
+// All blocks are 64 rows x 64 bf16 (128 bytes) with the 128-byte swizzle.
+// Swapping the two K halves' A blocks and negating the second gives i*C.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "tc.cuh"
+
+namespace pgb {
+namespace oz {
+
+constexpr int kBlk = 8192;            // one 64 x 64 bf16 block
+constexpr int kASlice = 3 * kBlk;     // [-A_i][A_r][A_i]
+constexpr int kBSlice = 2 * kBlk;     // [B_r^T][B_i^T]
+constexpr int kMaxSlices = 4;
+
+// Byte offset of bf16 element (row, k) in a 128-byte-swizzled K-major block.
+__device__ __forceinline__ uint32_t sw(int row, int k) {
+    return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((((k >> 3) ^ row) & 7) << 4) + ((k & 7) << 1));
+}
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, both operands
+// K-major, M = 128, N = 64; bit 13 negates A.
+__host__ __device__ constexpr uint32_t idesc_bf16(bool negate_a) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((negate_a ? 1u : 0u) << 13) | ((uint32_t)(64 >> 3) << 17) |
+           ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Issues the MMAs of one sliced product (one thread).  Slices s < sa_n of A
+// at sa (kASlice bytes each) and t < sb_n of B at sb (kBSlice each); level
+// L = s + t <= lmax accumulates at tmem column d_tmem + 64 L.  With imag set
+// the product is i * A * B.
+__device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint32_t sb, int sa_n, int sb_n,
+                                              int lmax, bool imag) {
+    const uint32_t id_pos = idesc_bf16(false), id_neg = idesc_bf16(true);
+    uint32_t started = 0;
+    for (int s = 0; s < sa_n; ++s) {
+        for (int t = 0; t < sb_n; ++t) {
+            const int L = s + t;
+            if (L > lmax) continue;
+            const uint32_t d = d_tmem + 64u * (uint32_t)L;
+            const uint32_t a = sa + (uint32_t)s * kASlice, b = sb + (uint32_t)t * kBSlice;
+            // K half 0: A' columns 0..63 = [A_r; A_i] (i*A: [-A_i; A_r]), B rows 0..63 = B_r.
+            const uint32_t a0 = imag ? a : a + kBlk;
+            // K half 1: [-A_i; A_r] (i*A: -[A_r; A_i]), B rows 64..127 = B_i.
+            const uint32_t a1 = imag ? a + kBlk : a;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), tc::desc_k_sw128(b + 32u * kk), id_pos,
+                         ((started >> L) & 1u) | (kk > 0 ? 1u : 0u));
+            }
+            started |= 1u << L;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), tc::desc_k_sw128(b + kBlk + 32u * kk),
+                         imag ? id_neg : id_pos, 1u);
+        }
+    }
+}
+
+// Exponent e with |v| < 2^e for every |v| <= m (0 for m == 0).
+__device__ __forceinline__ int scale_exp(float m) {
+    int e = 0;
+    if (m > 0.0f) frexpf(m, &e);
+    return e;
+}
+
+// Peels 8 scaled values (already multiplied by 2^(7 - e)) into up to S
+// slices; q[s][j] receives slice s of value j.
+template <int S>
+__device__ __forceinline__ void peel8(float (&t)[8], float (&q)[S][8]) {
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float r = rintf(t[j]);
+            q[s][j] = r;
+            t[j] = (t[j] - r) * 256.0f;
+        }
+}
+
+__device__ __forceinline__ uint4 pack8(const float (&v)[8], float sign) {
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(sign * v[2 * i], sign * v[2 * i + 1]);
+        w[i] = *reinterpret_cast<uint32_t *>(&h);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// Stores slices of 8 consecutive elements (row, k0..k0+7) of a real plane into
+// the A operand: plane 0 -> block A_r, plane 1 -> blocks A_i and -A_i.
+// k0 must be a multiple of 8.
+template <int S>
+__device__ __forceinline__ void store_a8(unsigned char *sa, int row, int k0, int plane, const float (&q)[S][8]) {
+    const uint32_t off = sw(row, k0);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        unsigned char *base = sa + s * kASlice;
+        if (plane == 0) {
+            *reinterpret_cast<uint4 *>(base + kBlk + off) = pack8(q[s], 1.0f);
+        } else {
+            *reinterpret_cast<uint4 *>(base + 2 * kBlk + off) = pack8(q[s], 1.0f);
+            *reinterpret_cast<uint4 *>(base + off) = pack8(q[s], -1.0f);
+        }
+    }
+}
+
+// Stores slices of 8 consecutive rows k0..k0+7 of column n of plane `plane`
+// of B into B^T (row n, K index 64 * plane + k).
+template <int S>
+__device__ __forceinline__ void store_b8(unsigned char *sb, int n, int k0, int plane, const float (&q)[S][8]) {
+    const uint32_t off = sw(n, k0) + (uint32_t)plane * kBlk;
+#pragma unroll
+    for (int s = 0; s < S; ++s) *reinterpret_cast<uint4 *>(sb + s * kBSlice + off) = pack8(q[s], 1.0f);
+}
+
+}  // namespace oz
+}  // namespace pgb

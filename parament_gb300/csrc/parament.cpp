@@ -370,6 +370,9 @@ static Parament_ErrorCode equiprop_host(Ctx *c, const void *carr, double dt, uns
     }
     if (!c->fp64 && c->dim > (unsigned)kSmallMaxDim && tc_take_faults() > 0)
         return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
+    if (!c->fp64 && c->precision == PARAMENT_PRECISION_SPLIT && split_tc_applies((int)c->dim, (int)c->Ke, c->last_M) &&
+        split_tc_take_faults() > 0)
+        return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
     return c->last_error = PARAMENT_STATUS_SUCCESS;
 }
 

@@ -1,0 +1,540 @@
+// Split-precision complex64 form on the tcgen05 tensor cores, d = 64.
+//
+// Same polynomial and the same chunked running product as k_split_steps
+// (split.cu): U_j = I + E_j with the reference's Chebyshev-Bessel polynomial
+// regrouped by powers of X_j, each CTA multiplying its chunk of consecutive
+// steps into E^P in double-float, the chunk products combined by the FP64
+// tree.  What changes is where the products run: every d^3 product is a
+// sliced bf16 product on the tensor cores (ozaki.cuh) whose levels accumulate
+// exactly in tensor memory.
+//
+//   * The polynomial terms are small: |mu_2 X^2| ~ (h ||X||)^2 and below.  X^2
+//     and X Q take three slices per operand (24 bits, six slice products),
+//     X^4 and X^6 two (three slice products).
+//   * The running product E E^P carries the whole propagator and is where
+//     FP32 rounding used to dominate the error (an emulation of the FP32
+//     kernel attributes over 99 % of its error to this one product); it takes
+//     four slices of each operand (ten slice products), exact to about 2^-29
+//     of the row and column scales.  Three slices of E^P measured 1.4e-6 at
+//     65536 steps, no better than FP32.
+//
+// The coefficients of the polynomial are real for even powers and imaginary
+// for odd ones (mu_n = m_n / Hnorm^n, m_n from J_0 + 2 sum (-i)^k J_k T_k),
+// so with Q = i N, N = sum nu_(2k+1) X^(2k), nu real, every update works on
+// one real plane at a time: the accumulators of the real-stacked product put
+// Re C in tensor-memory lanes 0..63 and Im C in lanes 64..127, and each thread
+// keeps the plane of its own lane for 32 columns.  X Q = i X N comes from the
+// same slices with the A blocks swapped (ozaki.cuh).  Only the first-order
+// term mu_1 X = i nu_1 X couples the planes; it is formed in double-float by
+// the assembly, which computes whole complex elements and hands each partner
+// thread its plane through shared memory.
+//
+// Layout of one CTA (256 threads, one per SM): shared memory holds the A
+// slices (4 x 24 KB), the B slices (4 x 16 KB) and a 48 KB exchange buffer;
+// tensor memory holds the product levels (columns 0..255) and E^P in
+// double-float (columns 256..383).  Every wait on the tensor core is bounded:
+// a wait that runs out stops the CTA, counts a fault and frees tensor memory.
+#include <math.h>
+#include <stdlib.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ctx.h"
+#include "kernels.h"
+#include "ozaki.cuh"
+#include "split_common.cuh"
+
+namespace pgb {
+
+constexpr int kTcdMaxKe = 64;
+// Slices per operand.  X^2 and X Q carry terms up to (h ||X||)^2 and need
+// three slices (24 bits); X^4, X^6 are two orders smaller and take two; the
+// running product takes four slices of each operand.
+constexpr int kTcdHi = 4;
+constexpr int kTcdX2 = 3;
+constexpr int kTcdG = 2;
+constexpr int kTcdRunB = 4;
+constexpr uint32_t kTcdWait = 1u << 24;
+constexpr size_t kTcdSA = (size_t)kTcdHi * oz::kASlice;
+constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
+constexpr size_t kTcdST = 48 * 256 * sizeof(float);
+constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdST + 1024;
+
+__device__ int g_split_tc_faults;
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// TMEM <- registers, 32 lanes x 16 columns (one warp).
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// E^P of this thread (32 columns, double-float) from / to tensor memory.
+__device__ __forceinline__ void load_ep(uint32_t taddr, float (&hi)[32], float (&lo)[32]) {
+    float v[16];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        tc::tmem_ld16(taddr + 16 * b, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (b < 2) hi[16 * b + j] = v[j];
+            else lo[16 * (b - 2) + j] = v[j];
+        }
+    }
+}
+__device__ __forceinline__ void store_ep(uint32_t taddr, const float (&hi)[32], const float (&lo)[32]) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = b < 2 ? hi[16 * b + j] : lo[16 * (b - 2) + j];
+        tmem_st16(taddr + 16 * b, v);
+    }
+    tmem_wait_st();
+}
+
+// Column maxima of a warp: v[j] holds this lane's value of column j; on
+// return v[0] holds the maximum over the 32 lanes of column `lane`.
+__device__ __forceinline__ void warp_column_max(float (&v)[32], int lane) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const float send = upper ? v[i] : v[i + o];
+            const float keep = upper ? v[i + o] : v[i];
+            v[i] = fmaxf(keep, __shfl_xor_sync(0xffffffffu, send, o));
+        }
+    }
+}
+
+// Peels scaled double-float values t = hi + lo (|t| < 128) into S slices.
+template <int S>
+__device__ __forceinline__ void peel8_df(const float (&hi)[8], const float (&lo)[8], float (&q)[S][8]) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float r0 = rintf(hi[j]);
+        q[0][j] = r0;
+        float t = ((hi[j] - r0) + lo[j]) * 256.0f;
+#pragma unroll
+        for (int s = 1; s < S; ++s) {
+            const float r = rintf(t);
+            q[s][j] = r;
+            t = (t - r) * 256.0f;
+        }
+    }
+}
+
+struct TcdShared {
+    float4 ws[kTcdMaxKe];
+    int amax[2][64], bmax[2][64];
+    int rowe[64], cole[64];
+    uint64_t bar;
+    uint32_t tmem_base;
+};
+
+// Per-thread view of the CTA: lane layout of the accumulators.  Thread
+// (warp w, lane l): tensor-memory lane rho = 32 (w % 4) + l, plane p = rho / 64
+// (0: real, 1: imaginary), matrix row r = rho % 64, columns c0 .. c0 + 31 with
+// c0 = 32 (w / 4).
+struct TcdThread {
+    int tid, lane, p, r, c0, hh;
+    uint32_t tm_acc, tm_ep;
+};
+
+// Row maxima -> exponents, then the A slices of this thread's 32 values.
+// `b` selects the max buffer; the other buffer is cleared for the next call.
+template <int S, bool DF>
+__device__ __forceinline__ void slice_a(TcdShared &sh, unsigned char *SA, const TcdThread &t, int b,
+                                        const float (&hi)[32], const float (&lo)[32]) {
+    float m = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) m = fmaxf(m, fabsf(hi[j]));
+    atomicMax(&sh.amax[b][t.r], __float_as_int(m));
+    __syncthreads();
+    const int e = oz::scale_exp(__int_as_float(sh.amax[b][t.r]));
+    if (t.p == 0 && t.hh == 0) sh.rowe[t.r] = e;
+    if (t.tid < 64) {
+        sh.amax[b ^ 1][t.tid] = 0;
+        sh.bmax[b ^ 1][t.tid] = 0;
+    }
+    const float sc = pow2f(7 - e);
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        float q[S][8];
+        float th[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) th[j] = hi[8 * g + j] * sc;
+        if (DF) {
+            float tl[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) tl[j] = lo[8 * g + j] * sc;
+            peel8_df<S>(th, tl, q);
+        } else {
+            oz::peel8<S>(th, q);
+        }
+        oz::store_a8<S>(SA, t.r, t.c0 + 8 * g, t.p, q);
+    }
+}
+
+// Column maxima -> exponents, then the B slices (row r of plane p is K index
+// r of block p of B^T, column c is row c of B^T).
+template <int S, bool DF>
+__device__ __forceinline__ void slice_b(TcdShared &sh, unsigned char *SB, const TcdThread &t, int b,
+                                        const float (&hi)[32], const float (&lo)[32]) {
+    {
+        float v[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = fabsf(hi[j]);
+        warp_column_max(v, t.lane);
+        atomicMax(&sh.bmax[b][t.c0 + t.lane], __float_as_int(v[0]));
+    }
+    __syncthreads();
+    if (t.p == 0 && t.r < 32) sh.cole[t.c0 + t.lane] = oz::scale_exp(__int_as_float(sh.bmax[b][t.c0 + t.lane]));
+    unsigned char *base = SB + t.p * oz::kBlk;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int e = oz::scale_exp(__int_as_float(sh.bmax[b][t.c0 + j]));
+        const float sc = pow2f(7 - e);
+        const uint32_t off = oz::sw(t.c0 + j, t.r);
+        float x = hi[j] * sc;
+        float r0 = rintf(x);
+        *reinterpret_cast<__nv_bfloat16 *>(base + off) = __float2bfloat16_rn(r0);
+        x = DF ? ((x - r0) + lo[j] * sc) * 256.0f : (x - r0) * 256.0f;
+#pragma unroll
+        for (int s = 1; s < S; ++s) {
+            const float rs = rintf(x);
+            *reinterpret_cast<__nv_bfloat16 *>(base + s * oz::kBSlice + off) = __float2bfloat16_rn(rs);
+            x = (x - rs) * 256.0f;
+        }
+    }
+}
+
+// Makes the slices visible to the tensor core, issues one sliced product and
+// waits for it.  Returns false (in every thread) if the wait gave up.
+__device__ __forceinline__ bool run_product(TcdShared &sh, const TcdThread &t, unsigned char *SA, unsigned char *SB,
+                                            int sa_n, int sb_n, int lmax, bool imag, uint32_t &ncommit) {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (t.tid == 0) {
+        oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag);
+        tc::mma_commit(&sh.bar);
+    }
+    const bool ok = tc::mbar_wait(&sh.bar, ncommit & 1, kTcdWait);
+    ++ncommit;
+    tc::fence_after_sync();
+    return __syncthreads_and(ok) != 0;
+}
+
+// Loads the levels of the last product for this thread's 32 columns and
+// combines them in FP32: v_j = 2^(e_r + e_c - 14) sum_L 2^(-8 L) D_L.
+__device__ __forceinline__ void epilogue_f(const TcdShared &sh, const TcdThread &t, int lmax, float (&out)[32]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float acc[16];
+        tc::tmem_ld16(t.tm_acc + 16 * h, acc);
+        for (int L = 1; L <= lmax; ++L) {
+            float v[16];
+            tc::tmem_ld16(t.tm_acc + 64 * L + 16 * h, v);
+            const float f = pow2f(-8 * L);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[j] = fmaf(v[j], f, acc[j]);
+        }
+        const int er = sh.rowe[t.r] - 14;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) out[16 * h + j] = acc[j] * pow2f(er + sh.cole[t.c0 + 16 * h + j]);
+    }
+}
+
+// Same for four levels in double-float.
+__device__ __forceinline__ void epilogue_df(const TcdShared &sh, const TcdThread &t, float (&hi)[32],
+                                            float (&lo)[32]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float d0[16], d1[16], d2[16], d3[16];
+        tc::tmem_ld16(t.tm_acc + 16 * h, d0);
+        tc::tmem_ld16(t.tm_acc + 64 + 16 * h, d1);
+        tc::tmem_ld16(t.tm_acc + 128 + 16 * h, d2);
+        tc::tmem_ld16(t.tm_acc + 192 + 16 * h, d3);
+        const int er = sh.rowe[t.r] - 14;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            float s, e;
+            two_sum(d0[j], d1[j] * 0.00390625f, s, e);
+            e = __fadd_rn(e, __fmaf_rn(d3[j], 5.9604644775390625e-8f, d2[j] * 1.52587890625e-5f));
+            const df v = df_norm(s, e);
+            const float sc = pow2f(er + sh.cole[t.c0 + 16 * h + j]);
+            hi[16 * h + j] = v.hi * sc;
+            lo[16 * h + j] = v.lo * sc;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256, 1) k_split_tc(const __grid_constant__ SplitArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem =
+        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char *SA = smem;
+    unsigned char *SB = smem + kTcdSA;
+    float *ST = reinterpret_cast<float *>(SB + kTcdSB);
+    __shared__ TcdShared sh;
+
+    const int warp = threadIdx.x >> 5;
+    TcdThread t;
+    t.tid = threadIdx.x;
+    t.lane = threadIdx.x & 31;
+    const int q4 = warp & 3;
+    t.hh = warp >> 2;
+    t.p = q4 >> 1;
+    t.r = 32 * (q4 & 1) + t.lane;
+    t.c0 = 32 * t.hh;
+    const long long s0 = a.P * blockIdx.x / a.nchunks;
+    const long long s1 = a.P * (blockIdx.x + 1) / a.nchunks;
+    const int M = a.M;
+
+    if (warp == 0) {
+        tc::tmem_alloc(&sh.tmem_base, 512);
+        tc::tmem_relinquish();
+    }
+    if (t.tid == 0) {
+        tc::mbar_init(&sh.bar, 1);
+        tc::fence_mbar_init();
+    }
+    if (t.tid < 64) {
+        sh.amax[0][t.tid] = sh.amax[1][t.tid] = 0;
+        sh.bmax[0][t.tid] = sh.bmax[1][t.tid] = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t lane_base = (uint32_t)(32 * q4) << 16;
+    t.tm_acc = sh.tmem_base + lane_base + (uint32_t)t.c0;
+    t.tm_ep = sh.tmem_base + lane_base + 256u + 64u * (uint32_t)t.hh;
+
+    // Coefficients: c0 = m_0 - 1 and even mu real, odd mu = i nu.
+    const df nu1 = df_from(a.mu[1].y);
+    const df mu2 = df_from(a.mu[2].x);
+    const float c0f_hi = df_from(a.c0.x).hi, c0f_lo = df_from(a.c0.x).lo;
+
+    uint32_t ncommit = 0;
+    int nb = 0;  // max-buffer parity
+    bool ok = true;
+    for (long long st = s0; st < s1; ++st) {
+        for (int m = t.tid; m < a.Ke; m += blockDim.x) {
+            const double2 w = split_weight(a, m, st);
+            const df re = df_from(w.x), im = df_from(w.y);
+            sh.ws[m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        }
+        __syncthreads();
+        // ---- assembly: whole complex elements of row r, columns cm .. cm + 15
+        float X[32], Eh[32], El[32];
+        {
+            const int cm = t.c0 + 16 * t.p;
+            cdf xa[16];
+            float2 sa[16];
+            {
+                const float4 *H0 = reinterpret_cast<const float4 *>(a.stack + t.r * 64 + cm);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const float4 v = H0[j];
+                    xa[2 * j] = cdf{{v.x, 0.f}, {v.y, 0.f}};
+                    xa[2 * j + 1] = cdf{{v.z, 0.f}, {v.w, 0.f}};
+                    sa[2 * j] = sa[2 * j + 1] = make_float2(0.f, 0.f);
+                }
+            }
+            for (int m = 0; m < a.Ke; ++m) {
+                const float4 *Hm = reinterpret_cast<const float4 *>(a.stack + (size_t)(m + 1) * 4096 + t.r * 64 + cm);
+                const float4 w = sh.ws[m];
+                float2 g[16];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const float4 v = Hm[j];
+                    g[2 * j] = make_float2(v.x, v.y);
+                    g[2 * j + 1] = make_float2(v.z, v.w);
+                }
+                if (m < a.K) {
+                    const cdf wd = {{w.x, w.y}, {w.z, w.w}};
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) xa[j] = cdf_add(xa[j], cdf_mul_c(wd, g[j]));
+                } else {
+                    const float2 wf = make_float2(w.x, w.z);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) cfma(sa[j], wf, g[j]);
+                }
+            }
+            // E = c0 I + i nu_1 X; keep plane p, send plane 1 - p to the partner (tid ^ 64).
+            float mx[16], meh[16], mel[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const cdf x = cdf_add_c(xa[j], sa[j]);
+                df er = df_neg(df_mul(nu1, x.im));
+                if (t.r == cm + j) er = df_add(er, df{c0f_hi, c0f_lo});
+                const df ei = df_mul(nu1, x.re);
+                const df mine = t.p ? ei : er, other = t.p ? er : ei;
+                mx[j] = t.p ? x.im.hi : x.re.hi;
+                meh[j] = mine.hi;
+                mel[j] = mine.lo;
+                ST[j * 256 + t.tid] = t.p ? x.re.hi : x.im.hi;
+                ST[(16 + j) * 256 + t.tid] = other.hi;
+                ST[(32 + j) * 256 + t.tid] = other.lo;
+            }
+            __syncthreads();
+            // Own half at columns 16 p .., the partner's at 16 (1 - p) ..
+            const int partner = t.tid ^ 64;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float rx = ST[j * 256 + partner], reh = ST[(16 + j) * 256 + partner],
+                            rel = ST[(32 + j) * 256 + partner];
+                X[j] = t.p ? rx : mx[j];
+                X[16 + j] = t.p ? mx[j] : rx;
+                Eh[j] = t.p ? reh : meh[j];
+                Eh[16 + j] = t.p ? meh[j] : reh;
+                El[j] = t.p ? rel : mel[j];
+                El[16 + j] = t.p ? mel[j] : rel;
+            }
+        }
+        // ---- X^2
+        float N[32], G[32];
+        slice_a<kTcdX2, false>(sh, SA, t, nb, X, X);
+        slice_b<kTcdX2, false>(sh, SB, t, nb, X, X);
+        nb ^= 1;
+        if (!(ok = run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit))) break;
+        epilogue_f(sh, t, kTcdX2 - 1, G);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const df v = df_add(df{Eh[j], El[j]}, df_mul_f(mu2, G[j]));
+            Eh[j] = v.hi;
+            El[j] = v.lo;
+            N[j] = (float)a.mu[3].y * G[j];
+        }
+        // ---- higher even powers X^(2k) = X^(2k-2) X^2
+        for (int k = 2; 2 * k <= M && ok; ++k) {
+            slice_a<kTcdG, false>(sh, SA, t, nb, G, G);
+            if (k == 2) slice_b<kTcdG, false>(sh, SB, t, nb, G, G);
+            nb ^= 1;
+            if (!(ok = run_product(sh, t, SA, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit))) break;
+            epilogue_f(sh, t, kTcdG - 1, G);
+            const float me = (float)a.mu[2 * k].x;
+            const float no = (2 * k + 1 <= M) ? (float)a.mu[2 * k + 1].y : 0.0f;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const df v = df_add_f(df{Eh[j], El[j]}, me * G[j]);
+                Eh[j] = v.hi;
+                El[j] = v.lo;
+                N[j] = fmaf(no, G[j], N[j]);
+            }
+        }
+        if (!ok) break;
+        // ---- odd part X Q = i X N
+        slice_a<kTcdX2, false>(sh, SA, t, nb, X, X);
+        slice_b<kTcdX2, false>(sh, SB, t, nb, N, N);
+        nb ^= 1;
+        if (!(ok = run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, true, ncommit))) break;
+        epilogue_f(sh, t, kTcdX2 - 1, G);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const df v = df_add_f(df{Eh[j], El[j]}, G[j]);
+            Eh[j] = v.hi;
+            El[j] = v.lo;
+        }
+        // ---- running product E^P <- E^P + E + E E^P
+        float Ph[32], Pl[32];
+        if (st == s0) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                Ph[j] = Eh[j];
+                Pl[j] = El[j];
+            }
+        } else {
+            load_ep(t.tm_ep, Ph, Pl);
+            slice_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
+            slice_b<kTcdRunB, true>(sh, SB, t, nb, Ph, Pl);
+            nb ^= 1;
+            if (!(ok = run_product(sh, t, SA, SB, kTcdHi, kTcdRunB, kTcdHi - 1, false, ncommit))) break;
+            epilogue_df(sh, t, G, N);  // G, N reused as the product's hi / lo
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                df v = df_add(df{Ph[j], Pl[j]}, df{Eh[j], El[j]});
+                v = df_add(v, df{G[j], N[j]});
+                Ph[j] = v.hi;
+                Pl[j] = v.lo;
+            }
+        }
+        store_ep(t.tm_ep, Ph, Pl);
+    }
+    if (ok && s1 > s0) {
+        // Chunk product I + E^P in complex128: plane p of row r, 32 columns.
+        float Ph[32], Pl[32];
+        load_ep(t.tm_ep, Ph, Pl);
+        double *dst = reinterpret_cast<double *>(a.chunks + (size_t)blockIdx.x * 4096);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int c = t.c0 + j;
+            double v = (double)Ph[j] + (double)Pl[j];
+            if (t.p == 0 && c == t.r) v += 1.0;
+            dst[2 * (t.r * 64 + c) + t.p] = v;
+        }
+    }
+    if (!ok) {
+        if (t.tid == 0) atomicAdd(&g_split_tc_faults, 1);
+        // Let any product still in flight finish before tensor memory is released.
+        tc::mbar_wait(&sh.bar, (ncommit - 1) & 1, kTcdWait);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(sh.tmem_base, 512);
+    }
+}
+
+static bool split_tc_disabled() {
+    static const bool off = [] {
+        const char *v = getenv("PARAMENT_DISABLE_TENSOR_CORES");
+        return v && v[0] && v[0] != '0';
+    }();
+    return off;
+}
+
+bool split_tc_applies(int d, int Ke, int M) {
+    return d == 64 && Ke <= kTcdMaxKe && M >= 3 && M <= kSplitMaxOrder && !split_tc_disabled();
+}
+
+cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, int *nchunks, cudaStream_t stream) {
+    cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_split_tc),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcdSmem);
+    if (e != cudaSuccess) return e;
+    SplitArgs b = a;
+    b.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)num_sms, a.P));
+    *nchunks = b.nchunks;
+    k_split_tc<<<b.nchunks, 256, kTcdSmem, stream>>>(b);
+    return cudaGetLastError();
+}
+
+int split_tc_take_faults() {
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_split_tc_faults, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (v) {
+        int z = 0;
+        cudaMemcpyToSymbol(g_split_tc_faults, &z, sizeof(int));
+    }
+    return v;
+}
+
+}  // namespace pgb
