@@ -29,16 +29,17 @@
 // the assembly, which computes whole complex elements and hands each partner
 // thread its plane through shared memory.
 //
-// Layout of one CTA (256 threads, one per SM): shared memory holds the A
+// Layout of one CTA (512 threads, one per SM): shared memory holds the A
 // slices (4 x 24 KB), the B slices (4 x 16 KB) and a 48 KB exchange buffer;
 // tensor memory holds the product levels (columns 0..255) and E^P in
-// double-float (columns 256..383).  Every wait on the tensor core is bounded:
+// double-float (columns 256..383).  Sixteen warps hide the latency of the
+// elementwise work (assembly, slicing, epilogues) that surrounds each
+// product; each thread owns one plane of 16 columns of one row.  Every wait on the tensor core is bounded:
 // a wait that runs out stops the CTA, counts a fault and frees tensor memory.
 #include <math.h>
 #include <stdlib.h>
 
 #include <algorithm>
-#include <vector>
 
 #include "ctx.h"
 #include "kernels.h"
@@ -47,6 +48,8 @@
 
 namespace pgb {
 
+constexpr int kTcdThreads = 512;
+constexpr int kTcdCols = 16;  // columns per thread
 constexpr int kTcdMaxKe = 64;
 // Slices per operand.  X^2 and X Q carry terms up to (h ||X||)^2 and need
 // three slices (24 bits); X^4, X^6 are two orders smaller and take two; the
@@ -54,16 +57,20 @@ constexpr int kTcdMaxKe = 64;
 constexpr int kTcdHi = 4;
 constexpr int kTcdX2 = 3;
 constexpr int kTcdG = 2;
-constexpr int kTcdRunB = 4;
 constexpr uint32_t kTcdWait = 1u << 24;
 constexpr size_t kTcdSA = (size_t)kTcdHi * oz::kASlice;
 constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
-constexpr size_t kTcdST = 48 * 256 * sizeof(float);
+constexpr int kTcdXch = 24;  // floats a thread hands its partner after the assembly
+constexpr size_t kTcdST = (size_t)kTcdXch * kTcdThreads * sizeof(float);
 constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdST + 1024;
 
 __device__ int g_split_tc_faults;
 
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// e with m < 2^e for the non-negative float whose bits are given (0 for m = 0;
+// at least -100, so that 2^(7 - e) stays finite).
+__device__ __forceinline__ int exp_above(int bits) { return bits == 0 ? 0 : max((bits >> 23) - 126, -100); }
 
 // TMEM <- registers, 32 lanes x 16 columns (one warp).
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
@@ -80,35 +87,11 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) 
 }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
-// E^P of this thread (32 columns, double-float) from / to tensor memory.
-__device__ __forceinline__ void load_ep(uint32_t taddr, float (&hi)[32], float (&lo)[32]) {
-    float v[16];
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        tc::tmem_ld16(taddr + 16 * b, v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            if (b < 2) hi[16 * b + j] = v[j];
-            else lo[16 * (b - 2) + j] = v[j];
-        }
-    }
-}
-__device__ __forceinline__ void store_ep(uint32_t taddr, const float (&hi)[32], const float (&lo)[32]) {
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        float v[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = b < 2 ? hi[16 * b + j] : lo[16 * (b - 2) + j];
-        tmem_st16(taddr + 16 * b, v);
-    }
-    tmem_wait_st();
-}
-
 // Column maxima of a warp: v[j] holds this lane's value of column j; on
-// return v[0] holds the maximum over the 32 lanes of column `lane`.
-__device__ __forceinline__ void warp_column_max(float (&v)[32], int lane) {
+// return v[0] holds the maximum over the 32 lanes of column lane % 16.
+__device__ __forceinline__ void warp_column_max(float (&v)[16], int lane) {
 #pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
+    for (int o = 8; o >= 1; o >>= 1) {
         const bool upper = (lane & o) != 0;
 #pragma unroll
         for (int i = 0; i < o; ++i) {
@@ -117,6 +100,7 @@ __device__ __forceinline__ void warp_column_max(float (&v)[32], int lane) {
             v[i] = fmaxf(keep, __shfl_xor_sync(0xffffffffu, send, o));
         }
     }
+    v[0] = fmaxf(v[0], __shfl_xor_sync(0xffffffffu, v[0], 16));
 }
 
 // Peels scaled double-float values t = hi + lo (|t| < 128) into S slices.
@@ -139,39 +123,40 @@ __device__ __forceinline__ void peel8_df(const float (&hi)[8], const float (&lo)
 struct TcdShared {
     float4 ws[kTcdMaxKe];
     int amax[2][64], bmax[2][64];
-    int rowe[64], cole[64];
+    float rowmul[64], colmul[64];  // 2^(e - 7) of the last A rows / B columns
+    int real_ctrl;                 // control weights of this step are real, commutator weights imaginary
     uint64_t bar;
     uint32_t tmem_base;
 };
 
 // Per-thread view of the CTA: lane layout of the accumulators.  Thread
 // (warp w, lane l): tensor-memory lane rho = 32 (w % 4) + l, plane p = rho / 64
-// (0: real, 1: imaginary), matrix row r = rho % 64, columns c0 .. c0 + 31 with
-// c0 = 32 (w / 4).
+// (0: real, 1: imaginary), matrix row r = rho % 64, columns c0 .. c0 + 15 with
+// c0 = 16 (w / 4).  Warps w and w ^ 2 hold the two planes of the same elements.
 struct TcdThread {
-    int tid, lane, p, r, c0, hh;
+    int tid, lane, p, r, c0, cb;
     uint32_t tm_acc, tm_ep;
 };
 
-// Row maxima -> exponents, then the A slices of this thread's 32 values.
+// Row maxima -> exponents, then the A slices of this thread's 16 values.
 // `b` selects the max buffer; the other buffer is cleared for the next call.
 template <int S, bool DF>
 __device__ __forceinline__ void slice_a(TcdShared &sh, unsigned char *SA, const TcdThread &t, int b,
-                                        const float (&hi)[32], const float (&lo)[32]) {
+                                        const float (&hi)[16], const float (&lo)[16]) {
     float m = 0.0f;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) m = fmaxf(m, fabsf(hi[j]));
+    for (int j = 0; j < 16; ++j) m = fmaxf(m, fabsf(hi[j]));
     atomicMax(&sh.amax[b][t.r], __float_as_int(m));
     __syncthreads();
-    const int e = oz::scale_exp(__int_as_float(sh.amax[b][t.r]));
-    if (t.p == 0 && t.hh == 0) sh.rowe[t.r] = e;
+    const int e = exp_above(sh.amax[b][t.r]);
+    if (t.p == 0 && t.cb == 0) sh.rowmul[t.r] = pow2f(e - 7);
     if (t.tid < 64) {
         sh.amax[b ^ 1][t.tid] = 0;
         sh.bmax[b ^ 1][t.tid] = 0;
     }
     const float sc = pow2f(7 - e);
 #pragma unroll
-    for (int g = 0; g < 4; ++g) {
+    for (int g = 0; g < 2; ++g) {
         float q[S][8];
         float th[8];
 #pragma unroll
@@ -192,24 +177,23 @@ __device__ __forceinline__ void slice_a(TcdShared &sh, unsigned char *SA, const 
 // r of block p of B^T, column c is row c of B^T).
 template <int S, bool DF>
 __device__ __forceinline__ void slice_b(TcdShared &sh, unsigned char *SB, const TcdThread &t, int b,
-                                        const float (&hi)[32], const float (&lo)[32]) {
+                                        const float (&hi)[16], const float (&lo)[16]) {
     {
-        float v[32];
+        float v[16];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = fabsf(hi[j]);
+        for (int j = 0; j < 16; ++j) v[j] = fabsf(hi[j]);
         warp_column_max(v, t.lane);
-        atomicMax(&sh.bmax[b][t.c0 + t.lane], __float_as_int(v[0]));
+        if (t.lane < 16) atomicMax(&sh.bmax[b][t.c0 + t.lane], __float_as_int(v[0]));
     }
     __syncthreads();
-    if (t.p == 0 && t.r < 32) sh.cole[t.c0 + t.lane] = oz::scale_exp(__int_as_float(sh.bmax[b][t.c0 + t.lane]));
+    if (t.p == 0 && t.r < 16) sh.colmul[t.c0 + t.lane] = pow2f(exp_above(sh.bmax[b][t.c0 + t.lane]) - 7);
     unsigned char *base = SB + t.p * oz::kBlk;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const int e = oz::scale_exp(__int_as_float(sh.bmax[b][t.c0 + j]));
-        const float sc = pow2f(7 - e);
+    for (int j = 0; j < 16; ++j) {
+        const float sc = pow2f(7 - exp_above(sh.bmax[b][t.c0 + j]));
         const uint32_t off = oz::sw(t.c0 + j, t.r);
         float x = hi[j] * sc;
-        float r0 = rintf(x);
+        const float r0 = rintf(x);
         *reinterpret_cast<__nv_bfloat16 *>(base + off) = __float2bfloat16_rn(r0);
         x = DF ? ((x - r0) + lo[j] * sc) * 256.0f : (x - r0) * 256.0f;
 #pragma unroll
@@ -239,51 +223,106 @@ __device__ __forceinline__ bool run_product(TcdShared &sh, const TcdThread &t, u
     return __syncthreads_and(ok) != 0;
 }
 
-// Loads the levels of the last product for this thread's 32 columns and
-// combines them in FP32: v_j = 2^(e_r + e_c - 14) sum_L 2^(-8 L) D_L.
-__device__ __forceinline__ void epilogue_f(const TcdShared &sh, const TcdThread &t, int lmax, float (&out)[32]) {
+// Loads the levels of the last product for this thread's 16 columns and
+// combines them in FP32: v_j = 2^(e_r - 7) 2^(e_c - 7) sum_L 2^(-8 L) D_L.
+template <int LMAX>
+__device__ __forceinline__ void epilogue_f(const TcdShared &sh, const TcdThread &t, float (&out)[16]) {
+    tc::tmem_ld16(t.tm_acc, out);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float acc[16];
-        tc::tmem_ld16(t.tm_acc + 16 * h, acc);
-        for (int L = 1; L <= lmax; ++L) {
-            float v[16];
-            tc::tmem_ld16(t.tm_acc + 64 * L + 16 * h, v);
-            const float f = pow2f(-8 * L);
+    for (int L = 1; L <= LMAX; ++L) {
+        float v[16];
+        tc::tmem_ld16(t.tm_acc + 64 * L, v);
+        const float f = pow2f(-8 * L);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j] = fmaf(v[j], f, acc[j]);
-        }
-        const int er = sh.rowe[t.r] - 14;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) out[16 * h + j] = acc[j] * pow2f(er + sh.cole[t.c0 + 16 * h + j]);
+        for (int j = 0; j < 16; ++j) out[j] = fmaf(v[j], f, out[j]);
     }
+    const float rm = sh.rowmul[t.r];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) out[j] *= rm * sh.colmul[t.c0 + j];
 }
 
-// Same for four levels in double-float.
-__device__ __forceinline__ void epilogue_df(const TcdShared &sh, const TcdThread &t, float (&hi)[32],
-                                            float (&lo)[32]) {
+// TMEM -> registers, 32 lanes x 8 columns (no wait).
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// The running product's four levels combined in double-float and added, with
+// E, to E^P (tensor memory): E^P <- E^P + E + 2^(e_r - 7) 2^(e_c - 7) sum_L 2^(-8 L) D_L.
+__device__ __forceinline__ void epilogue_running(const TcdShared &sh, const TcdThread &t, const float (&eh)[16],
+                                                 const float (&el)[16]) {
+    const float rm = sh.rowmul[t.r];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        float d0[16], d1[16], d2[16], d3[16];
-        tc::tmem_ld16(t.tm_acc + 16 * h, d0);
-        tc::tmem_ld16(t.tm_acc + 64 + 16 * h, d1);
-        tc::tmem_ld16(t.tm_acc + 128 + 16 * h, d2);
-        tc::tmem_ld16(t.tm_acc + 192 + 16 * h, d3);
-        const int er = sh.rowe[t.r] - 14;
+        float d0[8], d1[8], d2[8], d3[8], ph[8], pl[8];
+        tmem_ld8_nowait(t.tm_acc + 8 * h, d0);
+        tmem_ld8_nowait(t.tm_acc + 64 + 8 * h, d1);
+        tmem_ld8_nowait(t.tm_acc + 128 + 8 * h, d2);
+        tmem_ld8_nowait(t.tm_acc + 192 + 8 * h, d3);
+        tmem_ld8_nowait(t.tm_ep + 8 * h, ph);
+        tmem_ld8_nowait(t.tm_ep + 16 + 8 * h, pl);
+        tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
+        for (int j = 0; j < 8; ++j) {
             float s, e;
             two_sum(d0[j], d1[j] * 0.00390625f, s, e);
             e = __fadd_rn(e, __fmaf_rn(d3[j], 5.9604644775390625e-8f, d2[j] * 1.52587890625e-5f));
-            const df v = df_norm(s, e);
-            const float sc = pow2f(er + sh.cole[t.c0 + 16 * h + j]);
-            hi[16 * h + j] = v.hi * sc;
-            lo[16 * h + j] = v.lo * sc;
+            df v = df_norm(s, e);
+            const float sc = rm * sh.colmul[t.c0 + 8 * h + j];
+            v.hi *= sc;
+            v.lo *= sc;
+            df w = df_add(df{ph[j], pl[j]}, df{eh[8 * h + j], el[8 * h + j]});
+            w = df_add(w, v);
+            ph[j] = w.hi;
+            pl[j] = w.lo;
         }
+        uint32_t rh[8], rl[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            rh[j] = __float_as_uint(ph[j]);
+            rl[j] = __float_as_uint(pl[j]);
+        }
+        asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(t.tm_ep + 8 * h),
+                     "r"(rh[0]), "r"(rh[1]), "r"(rh[2]), "r"(rh[3]), "r"(rh[4]), "r"(rh[5]), "r"(rh[6]), "r"(rh[7])
+                     : "memory");
+        asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(
+                         t.tm_ep + 16 + 8 * h),
+                     "r"(rl[0]), "r"(rl[1]), "r"(rl[2]), "r"(rl[3]), "r"(rl[4]), "r"(rl[5]), "r"(rl[6]), "r"(rl[7])
+                     : "memory");
     }
+    tmem_wait_st();
 }
 
-__global__ void __launch_bounds__(256, 1) k_split_tc(const __grid_constant__ SplitArgs a) {
+// E^P of this thread (16 columns, double-float) from / to tensor memory.
+__device__ __forceinline__ void load_ep(uint32_t taddr, float (&hi)[16], float (&lo)[16]) {
+    tc::tmem_ld16(taddr, hi);
+    tc::tmem_ld16(taddr + 16, lo);
+}
+__device__ __forceinline__ void store_ep(uint32_t taddr, const float (&hi)[16], const float (&lo)[16]) {
+    tmem_st16(taddr, hi);
+    tmem_st16(taddr + 16, lo);
+    tmem_wait_st();
+}
+
+// acc += w h for a double-float real w and a float h; the compensation term
+// collects the rounding of the sum and the product without renormalising.
+__device__ __forceinline__ void df_mac_lazy(float &hi, float &lo, float wh, float wl, float h) {
+    const float p = __fmul_rn(wh, h);
+    float e = __fmaf_rn(wh, h, -p);
+    e = __fmaf_rn(wl, h, e);
+    float s, t;
+    two_sum(hi, p, s, t);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(t, e));
+}
+
+__global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_constant__ SplitArgs a) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -297,10 +336,10 @@ __global__ void __launch_bounds__(256, 1) k_split_tc(const __grid_constant__ Spl
     t.tid = threadIdx.x;
     t.lane = threadIdx.x & 31;
     const int q4 = warp & 3;
-    t.hh = warp >> 2;
+    t.cb = warp >> 2;
     t.p = q4 >> 1;
     t.r = 32 * (q4 & 1) + t.lane;
-    t.c0 = 32 * t.hh;
+    t.c0 = kTcdCols * t.cb;
     const long long s0 = a.P * blockIdx.x / a.nchunks;
     const long long s1 = a.P * (blockIdx.x + 1) / a.nchunks;
     const int M = a.M;
@@ -322,103 +361,140 @@ __global__ void __launch_bounds__(256, 1) k_split_tc(const __grid_constant__ Spl
     tc::fence_after_sync();
     const uint32_t lane_base = (uint32_t)(32 * q4) << 16;
     t.tm_acc = sh.tmem_base + lane_base + (uint32_t)t.c0;
-    t.tm_ep = sh.tmem_base + lane_base + 256u + 64u * (uint32_t)t.hh;
+    t.tm_ep = sh.tmem_base + lane_base + 256u + 32u * (uint32_t)t.cb;
 
     // Coefficients: c0 = m_0 - 1 and even mu real, odd mu = i nu.
     const df nu1 = df_from(a.mu[1].y);
     const df mu2 = df_from(a.mu[2].x);
-    const float c0f_hi = df_from(a.c0.x).hi, c0f_lo = df_from(a.c0.x).lo;
+    const df c0d = df_from(a.c0.x);
 
     uint32_t ncommit = 0;
     int nb = 0;  // max-buffer parity
     bool ok = true;
     for (long long st = s0; st < s1; ++st) {
+        if (t.tid == 0) sh.real_ctrl = 1;
+        __syncthreads();
         for (int m = t.tid; m < a.Ke; m += blockDim.x) {
             const double2 w = split_weight(a, m, st);
             const df re = df_from(w.x), im = df_from(w.y);
             sh.ws[m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+            if (m < a.K ? w.y != 0.0 : w.x != 0.0) sh.real_ctrl = 0;
         }
         __syncthreads();
-        // ---- assembly: whole complex elements of row r, columns cm .. cm + 15
-        float X[32], Eh[32], El[32];
+        // ---- assembly: whole complex elements of row r, columns cm .. cm + 7
+        float X[16], Eh[16], El[16];
         {
-            const int cm = t.c0 + 16 * t.p;
-            cdf xa[16];
-            float2 sa[16];
+            const int cm = t.c0 + 8 * t.p;
+            const size_t e0 = (size_t)t.r * 64 + cm;
+            float xrh[8], xrl[8], xih[8], xil[8], sr[8], si[8];
             {
-                const float4 *H0 = reinterpret_cast<const float4 *>(a.stack + t.r * 64 + cm);
+                const float4 *H0 = reinterpret_cast<const float4 *>(a.stack + e0);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
+                for (int j = 0; j < 4; ++j) {
                     const float4 v = H0[j];
-                    xa[2 * j] = cdf{{v.x, 0.f}, {v.y, 0.f}};
-                    xa[2 * j + 1] = cdf{{v.z, 0.f}, {v.w, 0.f}};
-                    sa[2 * j] = sa[2 * j + 1] = make_float2(0.f, 0.f);
+                    xrh[2 * j] = v.x;
+                    xih[2 * j] = v.y;
+                    xrh[2 * j + 1] = v.z;
+                    xih[2 * j + 1] = v.w;
                 }
-            }
-            for (int m = 0; m < a.Ke; ++m) {
-                const float4 *Hm = reinterpret_cast<const float4 *>(a.stack + (size_t)(m + 1) * 4096 + t.r * 64 + cm);
-                const float4 w = sh.ws[m];
-                float2 g[16];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
+                for (int j = 0; j < 8; ++j) xrl[j] = xil[j] = sr[j] = si[j] = 0.0f;
+            }
+            const bool real_ctrl = sh.real_ctrl != 0;
+            for (int m = 0; m < a.Ke; ++m) {
+                const float4 *Hm = reinterpret_cast<const float4 *>(a.stack + (size_t)(m + 1) * 4096 + e0);
+                const float4 w = sh.ws[m];
+                float gr[8], gi[8];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
                     const float4 v = Hm[j];
-                    g[2 * j] = make_float2(v.x, v.y);
-                    g[2 * j + 1] = make_float2(v.z, v.w);
+                    gr[2 * j] = v.x;
+                    gi[2 * j] = v.y;
+                    gr[2 * j + 1] = v.z;
+                    gi[2 * j + 1] = v.w;
                 }
                 if (m < a.K) {
-                    const cdf wd = {{w.x, w.y}, {w.z, w.w}};
+                    if (real_ctrl) {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) xa[j] = cdf_add(xa[j], cdf_mul_c(wd, g[j]));
+                        for (int j = 0; j < 8; ++j) {
+                            df_mac_lazy(xrh[j], xrl[j], w.x, w.y, gr[j]);
+                            df_mac_lazy(xih[j], xil[j], w.x, w.y, gi[j]);
+                        }
+                    } else {
+                        const cdf wd = {{w.x, w.y}, {w.z, w.w}};
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const cdf x = cdf_add(cdf{df_norm(xrh[j], xrl[j]), df_norm(xih[j], xil[j])},
+                                                  cdf_mul_c(wd, make_float2(gr[j], gi[j])));
+                            xrh[j] = x.re.hi;
+                            xrl[j] = x.re.lo;
+                            xih[j] = x.im.hi;
+                            xil[j] = x.im.lo;
+                        }
+                    }
+                } else if (real_ctrl) {
+                    // w = i v: w h = -v h_i + i v h_r
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        sr[j] = fmaf(-w.z, gi[j], sr[j]);
+                        si[j] = fmaf(w.z, gr[j], si[j]);
+                    }
                 } else {
-                    const float2 wf = make_float2(w.x, w.z);
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) cfma(sa[j], wf, g[j]);
+                    for (int j = 0; j < 8; ++j) {
+                        sr[j] = fmaf(w.x, gr[j], fmaf(-w.z, gi[j], sr[j]));
+                        si[j] = fmaf(w.x, gi[j], fmaf(w.z, gr[j], si[j]));
+                    }
                 }
             }
             // E = c0 I + i nu_1 X; keep plane p, send plane 1 - p to the partner (tid ^ 64).
-            float mx[16], meh[16], mel[16];
+            float mx[8], meh[8], mel[8];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const cdf x = cdf_add_c(xa[j], sa[j]);
-                df er = df_neg(df_mul(nu1, x.im));
-                if (t.r == cm + j) er = df_add(er, df{c0f_hi, c0f_lo});
-                const df ei = df_mul(nu1, x.re);
+            for (int j = 0; j < 8; ++j) {
+                const df xr = df_add_f(df_norm(xrh[j], xrl[j]), sr[j]);
+                const df xi = df_add_f(df_norm(xih[j], xil[j]), si[j]);
+                df er = df_neg(df_mul(nu1, xi));
+                if (t.r == cm + j) er = df_add(er, c0d);
+                const df ei = df_mul(nu1, xr);
                 const df mine = t.p ? ei : er, other = t.p ? er : ei;
-                mx[j] = t.p ? x.im.hi : x.re.hi;
+                mx[j] = t.p ? xi.hi : xr.hi;
                 meh[j] = mine.hi;
                 mel[j] = mine.lo;
-                ST[j * 256 + t.tid] = t.p ? x.re.hi : x.im.hi;
-                ST[(16 + j) * 256 + t.tid] = other.hi;
-                ST[(32 + j) * 256 + t.tid] = other.lo;
+                ST[j * kTcdThreads + t.tid] = t.p ? xr.hi : xi.hi;
+                ST[(8 + j) * kTcdThreads + t.tid] = other.hi;
+                ST[(16 + j) * kTcdThreads + t.tid] = other.lo;
             }
             __syncthreads();
-            // Own half at columns 16 p .., the partner's at 16 (1 - p) ..
+            // Own half at columns 8 p .., the partner's at 8 (1 - p) ..
             const int partner = t.tid ^ 64;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const float rx = ST[j * 256 + partner], reh = ST[(16 + j) * 256 + partner],
-                            rel = ST[(32 + j) * 256 + partner];
+            for (int j = 0; j < 8; ++j) {
+                const float rx = ST[j * kTcdThreads + partner], reh = ST[(8 + j) * kTcdThreads + partner],
+                            rel = ST[(16 + j) * kTcdThreads + partner];
                 X[j] = t.p ? rx : mx[j];
-                X[16 + j] = t.p ? mx[j] : rx;
+                X[8 + j] = t.p ? mx[j] : rx;
                 Eh[j] = t.p ? reh : meh[j];
-                Eh[16 + j] = t.p ? meh[j] : reh;
+                Eh[8 + j] = t.p ? meh[j] : reh;
                 El[j] = t.p ? rel : mel[j];
-                El[16 + j] = t.p ? mel[j] : rel;
+                El[8 + j] = t.p ? mel[j] : rel;
             }
         }
         // ---- X^2
-        float N[32], G[32];
+        float N[16], G[16];
         slice_a<kTcdX2, false>(sh, SA, t, nb, X, X);
         slice_b<kTcdX2, false>(sh, SB, t, nb, X, X);
         nb ^= 1;
         if (!(ok = run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit))) break;
-        epilogue_f(sh, t, kTcdX2 - 1, G);
+        epilogue_f<kTcdX2 - 1>(sh, t, G);
+        {
+            const float nu3 = (float)a.mu[3].y;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const df v = df_add(df{Eh[j], El[j]}, df_mul_f(mu2, G[j]));
-            Eh[j] = v.hi;
-            El[j] = v.lo;
-            N[j] = (float)a.mu[3].y * G[j];
+            for (int j = 0; j < 16; ++j) {
+                const df v = df_add(df{Eh[j], El[j]}, df_mul_f(mu2, G[j]));
+                Eh[j] = v.hi;
+                El[j] = v.lo;
+                N[j] = nu3 * G[j];
+            }
         }
         // ---- higher even powers X^(2k) = X^(2k-2) X^2
         for (int k = 2; 2 * k <= M && ok; ++k) {
@@ -426,11 +502,11 @@ __global__ void __launch_bounds__(256, 1) k_split_tc(const __grid_constant__ Spl
             if (k == 2) slice_b<kTcdG, false>(sh, SB, t, nb, G, G);
             nb ^= 1;
             if (!(ok = run_product(sh, t, SA, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit))) break;
-            epilogue_f(sh, t, kTcdG - 1, G);
+            epilogue_f<kTcdG - 1>(sh, t, G);
             const float me = (float)a.mu[2 * k].x;
             const float no = (2 * k + 1 <= M) ? (float)a.mu[2 * k + 1].y : 0.0f;
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
+            for (int j = 0; j < 16; ++j) {
                 const df v = df_add_f(df{Eh[j], El[j]}, me * G[j]);
                 Eh[j] = v.hi;
                 El[j] = v.lo;
@@ -443,45 +519,35 @@ __global__ void __launch_bounds__(256, 1) k_split_tc(const __grid_constant__ Spl
         slice_b<kTcdX2, false>(sh, SB, t, nb, N, N);
         nb ^= 1;
         if (!(ok = run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, true, ncommit))) break;
-        epilogue_f(sh, t, kTcdX2 - 1, G);
+        epilogue_f<kTcdX2 - 1>(sh, t, G);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
+        for (int j = 0; j < 16; ++j) {
             const df v = df_add_f(df{Eh[j], El[j]}, G[j]);
             Eh[j] = v.hi;
             El[j] = v.lo;
         }
         // ---- running product E^P <- E^P + E + E E^P
-        float Ph[32], Pl[32];
         if (st == s0) {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                Ph[j] = Eh[j];
-                Pl[j] = El[j];
-            }
+            store_ep(t.tm_ep, Eh, El);
         } else {
-            load_ep(t.tm_ep, Ph, Pl);
-            slice_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
-            slice_b<kTcdRunB, true>(sh, SB, t, nb, Ph, Pl);
-            nb ^= 1;
-            if (!(ok = run_product(sh, t, SA, SB, kTcdHi, kTcdRunB, kTcdHi - 1, false, ncommit))) break;
-            epilogue_df(sh, t, G, N);  // G, N reused as the product's hi / lo
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                df v = df_add(df{Ph[j], Pl[j]}, df{Eh[j], El[j]});
-                v = df_add(v, df{G[j], N[j]});
-                Ph[j] = v.hi;
-                Pl[j] = v.lo;
+            {
+                float Ph[16], Pl[16];
+                load_ep(t.tm_ep, Ph, Pl);
+                slice_b<kTcdHi, true>(sh, SB, t, nb, Ph, Pl);
             }
+            slice_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
+            nb ^= 1;
+            if (!(ok = run_product(sh, t, SA, SB, kTcdHi, kTcdHi, kTcdHi - 1, false, ncommit))) break;
+            epilogue_running(sh, t, Eh, El);
         }
-        store_ep(t.tm_ep, Ph, Pl);
     }
     if (ok && s1 > s0) {
-        // Chunk product I + E^P in complex128: plane p of row r, 32 columns.
-        float Ph[32], Pl[32];
+        // Chunk product I + E^P in complex128: plane p of row r, 16 columns.
+        float Ph[16], Pl[16];
         load_ep(t.tm_ep, Ph, Pl);
         double *dst = reinterpret_cast<double *>(a.chunks + (size_t)blockIdx.x * 4096);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
+        for (int j = 0; j < 16; ++j) {
             const int c = t.c0 + j;
             double v = (double)Ph[j] + (double)Pl[j];
             if (t.p == 0 && c == t.r) v += 1.0;
@@ -520,7 +586,7 @@ cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, int *nchunks, cudaS
     SplitArgs b = a;
     b.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)num_sms, a.P));
     *nchunks = b.nchunks;
-    k_split_tc<<<b.nchunks, 256, kTcdSmem, stream>>>(b);
+    k_split_tc<<<b.nchunks, kTcdThreads, kTcdSmem, stream>>>(b);
     return cudaGetLastError();
 }
 

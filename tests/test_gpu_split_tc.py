@@ -1,0 +1,99 @@
+"""The tensor-core split kernel (d = 64, complex64 contexts in split mode)
+against the FP64 oracle on the same complex64 inputs.
+
+The kernel forms every product from bf16 slices with exact accumulation and
+keeps the running product in double-float, so each case must land within the
+split form's bar of 1e-6 relative Frobenius error.  The cases cover the
+quadrature modes, the Magnus terms, complex samples (the general assembly
+branch), fewer steps than SMs, constant controls, and step sizes that push the
+Chebyshev order up to the split form's limit.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+QUAD = {oracle.NONE: "none", oracle.MIDPOINT: "midpoint", oracle.SIMPSON: "simpson"}
+TOL = 1e-6
+
+
+def c64(x):
+    return np.asarray(x).astype(np.complex64).astype(np.complex128)
+
+
+def relerr(a, b):
+    return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+
+def problem(K, n, seed, norm0=10.0, complex_samples=False):
+    from parament_gb300.workloads import hermitian
+    rng = np.random.default_rng(seed)
+    H0 = hermitian(rng, 64, norm0)
+    H1 = np.stack([hermitian(rng, 64, 1.0) for _ in range(K)]) if K else np.zeros((0, 64, 64), complex)
+    carr = rng.standard_normal((K, n)) + (1j * rng.standard_normal((K, n)) if complex_samples else 0)
+    return c64(H0), c64(H1), c64(carr)
+
+
+def split_equiprop(H0, H1, carr, dt, magnus, mode):
+    import parament_gb300 as parament
+    with parament.Parament("fp32") as ctx:
+        ctx.set_precision_mode("split")
+        ctx.set_hamiltonian(H0, *H1, use_magnus=magnus, quadrature_mode=QUAD[mode])
+        U = ctx.equiprop(dt, *carr)
+        return U.astype(np.complex128), ctx.last_iteration_cycles
+
+
+@pytest.mark.parametrize("magnus,mode", [(False, oracle.NONE), (False, oracle.MIDPOINT), (False, oracle.SIMPSON),
+                                         (True, oracle.SIMPSON)])
+@pytest.mark.parametrize("complex_samples", [False, True])
+def test_modes_and_samples(built_lib, magnus, mode, complex_samples):
+    H0, H1, carr = problem(3, 301, seed=11, complex_samples=complex_samples)
+    U, M = split_equiprop(H0, H1, list(carr), 1e-3, magnus, mode)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, magnus=magnus, mode=mode, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
+
+
+@pytest.mark.parametrize("steps", [1, 7, 151, 152, 153])
+def test_fewer_steps_than_sms(built_lib, steps):
+    H0, H1, carr = problem(2, steps, seed=steps)
+    U, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3)[0]
+    assert relerr(U, Uo) < TOL
+
+
+def test_constant_zero_controls(built_lib):
+    """Zero amplitudes: every step has X = H0, the same roundings each step."""
+    H0, H1, _ = problem(1, 1, seed=3, norm0=5.0)
+    carr = np.zeros((1, 400), np.complex128)
+    U, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3)[0]
+    assert relerr(U, Uo) < TOL
+
+
+@pytest.mark.parametrize("dt,order", [(1e-4, 3), (6e-3, 7), (1.6e-2, 9)])
+def test_chebyshev_orders(built_lib, dt, order):
+    """Larger steps raise the split order (more even powers in the kernel)."""
+    H0, H1, carr = problem(2, 257, seed=5, norm0=5.0)
+    U, M = split_equiprop(H0, H1, list(carr), dt, False, oracle.NONE)
+    Uo = oracle.equiprop(H0, H1, carr, dt, nthreads=os.cpu_count())[0]
+    assert M == order
+    assert relerr(U, Uo) < TOL, (M, relerr(U, Uo))
+
+
+def test_magnus_complex_samples_2048(built_lib):
+    H0, H1, carr = problem(4, 2 * 2048 + 1, seed=21, complex_samples=True)
+    U, M = split_equiprop(H0, H1, list(carr), 1e-3, True, oracle.SIMPSON)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, magnus=True, mode=oracle.SIMPSON, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
+
+
+def test_repeated_calls_agree(built_lib):
+    """The kernel keeps no state between calls: two calls give the same bits."""
+    H0, H1, carr = problem(2, 1000, seed=8)
+    U1, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
+    U2, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
+    assert np.array_equal(U1, U2)
