@@ -20,6 +20,9 @@
 // contiguous 128-row operand each.  B is stored K-major as [B_r^T | B_i^T].
 // All blocks are 64 rows x 64 bf16 (128 bytes) with the 128-byte swizzle.
 // Swapping the two K halves' A blocks and negating the second gives i*C.
+// B may instead be stored MN-major: rows k of [B_r; B_i] (128 of them) with
+// the 64 columns contiguous, the natural row-major layout, so that a thread
+// holding 8 consecutive columns of one row writes them with one 16-byte store.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -40,11 +43,24 @@ __device__ __forceinline__ uint32_t sw(int row, int k) {
     return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((((k >> 3) ^ row) & 7) << 4) + ((k & 7) << 1));
 }
 
-// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, both operands
-// K-major, M = 128, N = 64; bit 13 negates A.
-__host__ __device__ constexpr uint32_t idesc_bf16(bool negate_a) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((negate_a ? 1u : 0u) << 13) | ((uint32_t)(64 >> 3) << 17) |
-           ((uint32_t)(128 >> 4) << 24);
+// kind::f16 instruction descriptor: BF16 x BF16 -> FP32, A K-major, M = 128,
+// N = 64; bit 13 negates A, bit 16 selects an MN-major B.
+__host__ __device__ constexpr uint32_t idesc_bf16(bool negate_a, bool b_mn = false) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((negate_a ? 1u : 0u) << 13) | ((b_mn ? 1u : 0u) << 16) |
+           ((uint32_t)(64 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+// Shared-memory descriptor of an MN-major operand with the 128-byte swizzle
+// and 64 bf16 per row: one swizzle atom across N, 1024 bytes between groups of
+// eight K rows.
+__device__ __forceinline__ uint64_t desc_mn_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
@@ -58,12 +74,15 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
 }
 
 // Issues the MMAs of one sliced product (one thread).  Slices s < sa_n of A
-// at sa (kASlice bytes each) and t < sb_n of B at sb (kBSlice each); level
-// L = s + t <= lmax accumulates at tmem column d_tmem + 64 L.  With imag set
-// the product is i * A * B.
+// at sa (kASlice bytes each) and t < sb_n of B at sb (kBSlice each, K-major
+// or, with b_mn, MN-major); level L = s + t <= lmax accumulates at tmem
+// column d_tmem + 64 L.  With imag set the product is i * A * B.
 __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint32_t sb, int sa_n, int sb_n,
-                                              int lmax, bool imag) {
-    const uint32_t id_pos = idesc_bf16(false), id_neg = idesc_bf16(true);
+                                              int lmax, bool imag, bool b_mn = false) {
+    const uint32_t id_pos = idesc_bf16(false, b_mn), id_neg = idesc_bf16(true, b_mn);
+    // B address of K chunk kk (16 K values) within one K half: 32 bytes along
+    // a K-major row, or 16 rows of 128 bytes MN-major.
+    const uint32_t b_step = b_mn ? 2048u : 32u;
     uint32_t started = 0;
     for (int s = 0; s < sa_n; ++s) {
         for (int t = 0; t < sb_n; ++t) {
@@ -77,14 +96,17 @@ __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint
             const uint32_t a1 = imag ? a + kBlk : a;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-                mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), tc::desc_k_sw128(b + 32u * kk), id_pos,
+                const uint32_t bb = b + b_step * kk;
+                mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), b_mn ? desc_mn_sw128(bb) : tc::desc_k_sw128(bb), id_pos,
                          ((started >> L) & 1u) | (kk > 0 ? 1u : 0u));
             }
             started |= 1u << L;
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk)
-                mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), tc::desc_k_sw128(b + kBlk + 32u * kk),
+            for (int kk = 0; kk < 4; ++kk) {
+                const uint32_t bb = b + kBlk + b_step * kk;
+                mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), b_mn ? desc_mn_sw128(bb) : tc::desc_k_sw128(bb),
                          imag ? id_neg : id_pos, 1u);
+            }
         }
     }
 }

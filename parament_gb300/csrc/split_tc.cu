@@ -121,10 +121,9 @@ __device__ __forceinline__ void peel8_df(const float (&hi)[8], const float (&lo)
 }
 
 struct TcdShared {
-    float4 ws[kTcdMaxKe];
+    float4 ws[2][kTcdMaxKe];       // step weights (double-float re, im), double-buffered across steps
     int amax[2][64], bmax[2][64];
     float rowmul[64], colmul[64];  // 2^(e - 7) of the last A rows / B columns
-    int real_ctrl;                 // control weights of this step are real, commutator weights imaginary
     uint64_t bar;
     uint32_t tmem_base;
 };
@@ -138,22 +137,38 @@ struct TcdThread {
     uint32_t tm_acc, tm_ep;
 };
 
-// Row maxima -> exponents, then the A slices of this thread's 16 values.
-// `b` selects the max buffer; the other buffer is cleared for the next call.
-template <int S, bool DF>
-__device__ __forceinline__ void slice_a(TcdShared &sh, unsigned char *SA, const TcdThread &t, int b,
-                                        const float (&hi)[16], const float (&lo)[16]) {
-    float m = 0.0f;
+// Operand slicing.  reduce_max() posts this thread's row maximum of the A
+// values and (HAS_B) column maxima of the B values; after one barrier,
+// store_a() / store_b() write the slices.  `b` selects the max
+// buffer; the other buffer is cleared for the next product.
+template <bool HAS_A, bool HAS_B>
+__device__ __forceinline__ void reduce_max(TcdShared &sh, const TcdThread &t, int b, const float (&a)[16],
+                                           const float (&bv)[16]) {
+    if (HAS_A) {
+        float m = 0.0f;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) m = fmaxf(m, fabsf(hi[j]));
-    atomicMax(&sh.amax[b][t.r], __float_as_int(m));
+        for (int j = 0; j < 16; ++j) m = fmaxf(m, fabsf(a[j]));
+        atomicMax(&sh.amax[b][t.r], __float_as_int(m));
+    }
+    if (HAS_B) {
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = fabsf(bv[j]);
+        warp_column_max(v, t.lane);
+        if (t.lane < 16) atomicMax(&sh.bmax[b][t.c0 + t.lane], __float_as_int(v[0]));
+    }
     __syncthreads();
-    const int e = exp_above(sh.amax[b][t.r]);
-    if (t.p == 0 && t.cb == 0) sh.rowmul[t.r] = pow2f(e - 7);
     if (t.tid < 64) {
         sh.amax[b ^ 1][t.tid] = 0;
         sh.bmax[b ^ 1][t.tid] = 0;
     }
+}
+
+template <int S, bool DF>
+__device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const TcdThread &t, int b,
+                                        const float (&hi)[16], const float (&lo)[16]) {
+    const int e = exp_above(sh.amax[b][t.r]);
+    if (t.p == 0 && t.cb == 0) sh.rowmul[t.r] = pow2f(e - 7);
     const float sc = pow2f(7 - e);
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
@@ -173,72 +188,87 @@ __device__ __forceinline__ void slice_a(TcdShared &sh, unsigned char *SA, const 
     }
 }
 
-// Column maxima -> exponents, then the B slices (row r of plane p is K index
-// r of block p of B^T, column c is row c of B^T).
+// B slices, MN-major: row r of plane p is K row 64 p + r of [B_r; B_i], the
+// thread's 16 columns are contiguous within it.
 template <int S, bool DF>
-__device__ __forceinline__ void slice_b(TcdShared &sh, unsigned char *SB, const TcdThread &t, int b,
+__device__ __forceinline__ void store_b(TcdShared &sh, unsigned char *SB, const TcdThread &t, int b,
                                         const float (&hi)[16], const float (&lo)[16]) {
-    {
-        float v[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = fabsf(hi[j]);
-        warp_column_max(v, t.lane);
-        if (t.lane < 16) atomicMax(&sh.bmax[b][t.c0 + t.lane], __float_as_int(v[0]));
-    }
-    __syncthreads();
     if (t.p == 0 && t.r < 16) sh.colmul[t.c0 + t.lane] = pow2f(exp_above(sh.bmax[b][t.c0 + t.lane]) - 7);
-    unsigned char *base = SB + t.p * oz::kBlk;
+    const int k = 64 * t.p + t.r;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const float sc = pow2f(7 - exp_above(sh.bmax[b][t.c0 + j]));
-        const uint32_t off = oz::sw(t.c0 + j, t.r);
-        float x = hi[j] * sc;
-        const float r0 = rintf(x);
-        *reinterpret_cast<__nv_bfloat16 *>(base + off) = __float2bfloat16_rn(r0);
-        x = DF ? ((x - r0) + lo[j] * sc) * 256.0f : (x - r0) * 256.0f;
+    for (int g = 0; g < 2; ++g) {
+        float th[8], q[S][8];
+        if (DF) {
+            float tl[8];
 #pragma unroll
-        for (int s = 1; s < S; ++s) {
-            const float rs = rintf(x);
-            *reinterpret_cast<__nv_bfloat16 *>(base + s * oz::kBSlice + off) = __float2bfloat16_rn(rs);
-            x = (x - rs) * 256.0f;
+            for (int j = 0; j < 8; ++j) {
+                const float sc = pow2f(7 - exp_above(sh.bmax[b][t.c0 + 8 * g + j]));
+                th[j] = hi[8 * g + j] * sc;
+                tl[j] = lo[8 * g + j] * sc;
+            }
+            peel8_df<S>(th, tl, q);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) th[j] = hi[8 * g + j] * pow2f(7 - exp_above(sh.bmax[b][t.c0 + 8 * g + j]));
+            oz::peel8<S>(th, q);
         }
+        const uint32_t off = oz::sw(k, t.c0 + 8 * g);
+#pragma unroll
+        for (int s = 0; s < S; ++s) *reinterpret_cast<uint4 *>(SB + s * oz::kBSlice + off) = oz::pack8(q[s], 1.0f);
     }
 }
 
 // Makes the slices visible to the tensor core, issues one sliced product and
-// waits for it.  Returns false (in every thread) if the wait gave up.
+// waits for it.  `ok` carries this thread's result of the previous wait; the
+// barrier before the issue combines it over the CTA, and a product is issued
+// only if every earlier wait succeeded (returns false otherwise, in every
+// thread).
 __device__ __forceinline__ bool run_product(TcdShared &sh, const TcdThread &t, unsigned char *SA, unsigned char *SB,
-                                            int sa_n, int sb_n, int lmax, bool imag, uint32_t &ncommit) {
+                                            int sa_n, int sb_n, int lmax, bool imag, uint32_t &ncommit, bool &ok) {
     tc::fence_proxy_async();
     tc::fence_before_sync();
-    __syncthreads();
+    const bool all_ok = __syncthreads_and(ok) != 0;
     tc::fence_after_sync();
+    if (!all_ok) return false;
     if (t.tid == 0) {
-        oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag);
+        oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, true);
         tc::mma_commit(&sh.bar);
     }
-    const bool ok = tc::mbar_wait(&sh.bar, ncommit & 1, kTcdWait);
+    ok = tc::mbar_wait(&sh.bar, ncommit & 1, kTcdWait);
     ++ncommit;
     tc::fence_after_sync();
-    return __syncthreads_and(ok) != 0;
+    return true;
+}
+
+// TMEM -> registers, 32 lanes x 16 columns (no wait).
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // Loads the levels of the last product for this thread's 16 columns and
 // combines them in FP32: v_j = 2^(e_r - 7) 2^(e_c - 7) sum_L 2^(-8 L) D_L.
 template <int LMAX>
 __device__ __forceinline__ void epilogue_f(const TcdShared &sh, const TcdThread &t, float (&out)[16]) {
-    tc::tmem_ld16(t.tm_acc, out);
+    float lv[LMAX + 1][16];
 #pragma unroll
-    for (int L = 1; L <= LMAX; ++L) {
-        float v[16];
-        tc::tmem_ld16(t.tm_acc + 64 * L, v);
-        const float f = pow2f(-8 * L);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) out[j] = fmaf(v[j], f, out[j]);
-    }
+    for (int L = 0; L <= LMAX; ++L) tmem_ld16_nowait(t.tm_acc + 64 * L, lv[L]);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const float rm = sh.rowmul[t.r];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) out[j] *= rm * sh.colmul[t.c0 + j];
+    for (int j = 0; j < 16; ++j) {
+        float v = lv[LMAX][j];
+#pragma unroll
+        for (int L = LMAX - 1; L >= 0; --L) v = fmaf(v, 0.00390625f, lv[L][j]);
+        out[j] = v * (rm * sh.colmul[t.c0 + j]);
+    }
 }
 
 // TMEM -> registers, 32 lanes x 8 columns (no wait).
@@ -371,16 +401,19 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     uint32_t ncommit = 0;
     int nb = 0;  // max-buffer parity
     bool ok = true;
-    for (long long st = s0; st < s1; ++st) {
-        if (t.tid == 0) sh.real_ctrl = 1;
-        __syncthreads();
+    // Step weights are computed one step ahead by the first Ke threads, so
+    // their sample loads overlap the previous step's products.
+    auto weights = [&](long long st, int buf) {
         for (int m = t.tid; m < a.Ke; m += blockDim.x) {
             const double2 w = split_weight(a, m, st);
             const df re = df_from(w.x), im = df_from(w.y);
-            sh.ws[m] = make_float4(re.hi, re.lo, im.hi, im.lo);
-            if (m < a.K ? w.y != 0.0 : w.x != 0.0) sh.real_ctrl = 0;
+            sh.ws[buf][m] = make_float4(re.hi, re.lo, im.hi, im.lo);
         }
-        __syncthreads();
+    };
+    if (s1 > s0) weights(s0, 0);
+    __syncthreads();
+    for (long long st = s0; st < s1; ++st) {
+        const int wb = (int)((st - s0) & 1);
         // ---- assembly: whole complex elements of row r, columns cm .. cm + 7
         float X[16], Eh[16], El[16];
         {
@@ -400,10 +433,9 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
 #pragma unroll
                 for (int j = 0; j < 8; ++j) xrl[j] = xil[j] = sr[j] = si[j] = 0.0f;
             }
-            const bool real_ctrl = sh.real_ctrl != 0;
             for (int m = 0; m < a.Ke; ++m) {
                 const float4 *Hm = reinterpret_cast<const float4 *>(a.stack + (size_t)(m + 1) * 4096 + e0);
-                const float4 w = sh.ws[m];
+                const float4 w = sh.ws[wb][m];
                 float gr[8], gi[8];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -413,8 +445,9 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                     gr[2 * j + 1] = v.z;
                     gi[2 * j + 1] = v.w;
                 }
+                // The branches depend on the slot's weight only: uniform over the CTA.
                 if (m < a.K) {
-                    if (real_ctrl) {
+                    if (w.z == 0.0f && w.w == 0.0f) {  // real weight (real control samples)
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
                             df_mac_lazy(xrh[j], xrl[j], w.x, w.y, gr[j]);
@@ -432,8 +465,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                             xil[j] = x.im.lo;
                         }
                     }
-                } else if (real_ctrl) {
-                    // w = i v: w h = -v h_i + i v h_r
+                } else if (w.x == 0.0f) {
+                    // commutator slot with an imaginary weight i v: w h = -v h_i + i v h_r
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         sr[j] = fmaf(-w.z, gi[j], sr[j]);
@@ -465,6 +498,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                 ST[(16 + j) * kTcdThreads + t.tid] = other.lo;
             }
             __syncthreads();
+            // The next step's weights: every thread is past this step's assembly.
+            if (st + 1 < s1) weights(st + 1, wb ^ 1);
             // Own half at columns 8 p .., the partner's at 8 (1 - p) ..
             const int partner = t.tid ^ 64;
 #pragma unroll
@@ -481,10 +516,11 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         }
         // ---- X^2
         float N[16], G[16];
-        slice_a<kTcdX2, false>(sh, SA, t, nb, X, X);
-        slice_b<kTcdX2, false>(sh, SB, t, nb, X, X);
+        reduce_max<true, true>(sh, t, nb, X, X);
+        store_a<kTcdX2, false>(sh, SA, t, nb, X, X);
+        store_b<kTcdX2, false>(sh, SB, t, nb, X, X);
         nb ^= 1;
-        if (!(ok = run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit))) break;
+        if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit, ok)) break;
         epilogue_f<kTcdX2 - 1>(sh, t, G);
         {
             const float nu3 = (float)a.mu[3].y;
@@ -497,11 +533,16 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             }
         }
         // ---- higher even powers X^(2k) = X^(2k-2) X^2
-        for (int k = 2; 2 * k <= M && ok; ++k) {
-            slice_a<kTcdG, false>(sh, SA, t, nb, G, G);
-            if (k == 2) slice_b<kTcdG, false>(sh, SB, t, nb, G, G);
+        bool live = true;
+        for (int k = 2; 2 * k <= M; ++k) {
+            if (k == 2)
+                reduce_max<true, true>(sh, t, nb, G, G);
+            else
+                reduce_max<true, false>(sh, t, nb, G, G);
+            store_a<kTcdG, false>(sh, SA, t, nb, G, G);
+            if (k == 2) store_b<kTcdG, false>(sh, SB, t, nb, G, G);
             nb ^= 1;
-            if (!(ok = run_product(sh, t, SA, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit))) break;
+            if (!(live = run_product(sh, t, SA, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok))) break;
             epilogue_f<kTcdG - 1>(sh, t, G);
             const float me = (float)a.mu[2 * k].x;
             const float no = (2 * k + 1 <= M) ? (float)a.mu[2 * k + 1].y : 0.0f;
@@ -513,12 +554,13 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                 N[j] = fmaf(no, G[j], N[j]);
             }
         }
-        if (!ok) break;
+        if (!live) break;
         // ---- odd part X Q = i X N
-        slice_a<kTcdX2, false>(sh, SA, t, nb, X, X);
-        slice_b<kTcdX2, false>(sh, SB, t, nb, N, N);
+        reduce_max<true, true>(sh, t, nb, X, N);
+        store_a<kTcdX2, false>(sh, SA, t, nb, X, X);
+        store_b<kTcdX2, false>(sh, SB, t, nb, N, N);
         nb ^= 1;
-        if (!(ok = run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, true, ncommit))) break;
+        if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, true, ncommit, ok)) break;
         epilogue_f<kTcdX2 - 1>(sh, t, G);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -533,14 +575,17 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             {
                 float Ph[16], Pl[16];
                 load_ep(t.tm_ep, Ph, Pl);
-                slice_b<kTcdHi, true>(sh, SB, t, nb, Ph, Pl);
+                reduce_max<true, true>(sh, t, nb, Eh, Ph);
+                store_b<kTcdHi, true>(sh, SB, t, nb, Ph, Pl);
             }
-            slice_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
+            store_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
             nb ^= 1;
-            if (!(ok = run_product(sh, t, SA, SB, kTcdHi, kTcdHi, kTcdHi - 1, false, ncommit))) break;
+            if (!run_product(sh, t, SA, SB, kTcdHi, kTcdHi, kTcdHi - 1, false, ncommit, ok)) break;
             epilogue_running(sh, t, Eh, El);
         }
     }
+    // The last product's wait, combined over the CTA.
+    ok = __syncthreads_and(ok) != 0;
     if (ok && s1 > s0) {
         // Chunk product I + E^P in complex128: plane p of row r, 16 columns.
         float Ph[16], Pl[16];
