@@ -157,10 +157,11 @@ def library_gemm_peaks(torch):
 
 
 def flops_per_step(d, M, Ke, form):
-    """Algorithmic flops of one time step: M complex d^3 products (M-1 Clenshaw
-    products after the scalar first term, plus the running product), the
-    assembly (Ke complex multiply-adds per element).  The split form evaluates
-    the same polynomial with its own product count."""
+    """Algorithmic flops of one time step: M complex d^3 products for the
+    reference scheme (M-1 Clenshaw products after the scalar first term, plus
+    the running product) and the assembly (Ke complex multiply-adds per
+    element).  The split form evaluates the same polynomial with its own
+    product count."""
     gemm = 8.0 * d ** 3
     if form == "split_c64":
         return gemm * split_products(M) + 8.0 * Ke * d * d
@@ -168,11 +169,18 @@ def flops_per_step(d, M, Ke, form):
 
 
 def split_products(M):
-    """d^3 complex products per step of the split form: X^2 as hi*hi plus the
-    two cross products, the even powers X^4..X^(M-1), the odd part X*Q and
-    the running product."""
+    """Complex d^3 products per step of the split form at d = 64 (the
+    tensor-core kernel): X^2, the even powers X^4..X^(M-1), the odd part X Q
+    and the running product."""
+    return (M - 1) // 2 + 2
+
+
+# bf16 slice products the tensor-core split kernel issues per algorithmic
+# product: X^2 and X Q three slices per operand (6 slice products), the higher
+# even powers two (3), the running product four (10).
+def split_slice_products(M):
     q = (M - 1) // 2
-    return 3 + max(0, q - 1) + 1 + 1
+    return 6 + 3 * max(0, q - 1) + 6 + 10
 
 
 def run_form(torch, parament, w, form, K, W, flush, stream):
@@ -512,6 +520,11 @@ def run_ours(args, rank, world, local):
     fl = flops_per_step(d, M, Ke, head) * P
     achieved = fl / (kms * 1e-3) / 1e12
     pipe_peak = lib_peaks["fp64_gemm_tflops"] if head == "plain_c128" else lib_peaks["fp32_gemm_tflops"]
+    issued = None
+    if head == "split_c64":
+        # Issued tensor work: bf16 slice products of the real-stacked form
+        # (M = 128, N = 64, K = 128 real: 2 * 128 * 64 * 128 = 8 d^3 flop each).
+        issued = split_slice_products(M) * 8.0 * d ** 3 * P / (kms * 1e-3) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
@@ -536,9 +549,11 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "tensor", "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"],
                      "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 5), "traffic": traffic,
                      "peak_source": f"{peak_src} bf16 dense (MEASURED_PEAKS.json)",
-                     "kernel": "k_small_steps" if head != "split_c64" else "k_split_steps",
+                     "kernel": "k_small_steps" if head != "split_c64" else "k_split_tc",
                      "algorithmic_flops_per_launch": fl, "kernel_ms": round(kms, 4),
-                     "pipe": "fp64" if head == "plain_c128" else "fp32",
+                     "issued_bf16_tflops": round(issued, 2) if issued else None,
+                     "issued_bf16_frac": round(issued / peaks["bf16_tflops"], 4) if issued else None,
+                     "pipe": "fp64" if head == "plain_c128" else ("tensor (bf16 slices)" if head == "split_c64" else "fp32"),
                      "pipe_peak_tflops": pipe_peak, "pipe_frac": round(achieved / pipe_peak, 4),
                      "pipe_peak_source": "cuBLAS GEMM 8192^3 measured in this run", **lib_peaks},
         "clocks": clk.summary(),

@@ -66,12 +66,6 @@ constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdST + 1024;
 
 __device__ int g_split_tc_faults;
 
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
-
-// e with m < 2^e for the non-negative float whose bits are given (0 for m = 0;
-// at least -100, so that 2^(7 - e) stays finite).
-__device__ __forceinline__ int exp_above(int bits) { return bits == 0 ? 0 : max((bits >> 23) - 126, -100); }
-
 // TMEM <- registers, 32 lanes x 16 columns (one warp).
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
     asm volatile(
@@ -164,12 +158,23 @@ __device__ __forceinline__ void reduce_max(TcdShared &sh, const TcdThread &t, in
     }
 }
 
+// Scale that brings values of magnitude below the maximum m (float bits) under
+// 128: 2^(7 - e) with m < 2^e, from the exponent field alone (maxima below
+// 2^-100, zero included, are treated as 2^-100).
+__device__ __forceinline__ float scale_of(int mbits) {
+    return __int_as_float((260 << 23) - (max(mbits, 27 << 23) & 0x7F800000));
+}
+// Its inverse 2^(e - 7), the factor the epilogue applies.
+__device__ __forceinline__ float unscale_of(int mbits) {
+    return __int_as_float((max(mbits, 27 << 23) & 0x7F800000) - (6 << 23));
+}
+
 template <int S, bool DF>
 __device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const TcdThread &t, int b,
                                         const float (&hi)[16], const float (&lo)[16]) {
-    const int e = exp_above(sh.amax[b][t.r]);
-    if (t.p == 0 && t.cb == 0) sh.rowmul[t.r] = pow2f(e - 7);
-    const float sc = pow2f(7 - e);
+    const int mb = sh.amax[b][t.r];
+    if (t.p == 0 && t.cb == 0) sh.rowmul[t.r] = unscale_of(mb);
+    const float sc = scale_of(mb);
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
         float q[S][8];
@@ -193,23 +198,23 @@ __device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const 
 template <int S, bool DF>
 __device__ __forceinline__ void store_b(TcdShared &sh, unsigned char *SB, const TcdThread &t, int b,
                                         const float (&hi)[16], const float (&lo)[16]) {
-    if (t.p == 0 && t.r < 16) sh.colmul[t.c0 + t.lane] = pow2f(exp_above(sh.bmax[b][t.c0 + t.lane]) - 7);
+    if (t.p == 0 && t.r < 16) sh.colmul[t.c0 + t.lane] = unscale_of(sh.bmax[b][t.c0 + t.lane]);
     const int k = 64 * t.p + t.r;
+    const int4 *cm = reinterpret_cast<const int4 *>(sh.bmax[b] + t.c0);
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
+        const int4 m0 = cm[2 * g], m1 = cm[2 * g + 1];
+        const float sc[8] = {scale_of(m0.x), scale_of(m0.y), scale_of(m0.z), scale_of(m0.w),
+                             scale_of(m1.x), scale_of(m1.y), scale_of(m1.z), scale_of(m1.w)};
         float th[8], q[S][8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) th[j] = hi[8 * g + j] * sc[j];
         if (DF) {
             float tl[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const float sc = pow2f(7 - exp_above(sh.bmax[b][t.c0 + 8 * g + j]));
-                th[j] = hi[8 * g + j] * sc;
-                tl[j] = lo[8 * g + j] * sc;
-            }
+            for (int j = 0; j < 8; ++j) tl[j] = lo[8 * g + j] * sc[j];
             peel8_df<S>(th, tl, q);
         } else {
-#pragma unroll
-            for (int j = 0; j < 8; ++j) th[j] = hi[8 * g + j] * pow2f(7 - exp_above(sh.bmax[b][t.c0 + 8 * g + j]));
             oz::peel8<S>(th, q);
         }
         const uint32_t off = oz::sw(k, t.c0 + 8 * g);
