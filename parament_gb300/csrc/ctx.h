@@ -54,7 +54,7 @@ struct Ctx {
     int launches = 0;
 
     // Work buffers (grow-only, like src/cuda/parament.cpp:418-474)
-    DevBuf carr, out, chunks, work, X, B1, B2, aux, grad;
+    DevBuf carr, out, chunks, work, X, B1, B2, aux, grad, wts;
 
     size_t esize() const { return fp64 ? 16 : 8; }
     void release_all() {
@@ -69,6 +69,7 @@ struct Ctx {
         B2.release();
         aux.release();
         grad.release();
+        wts.release();
     }
 };
 

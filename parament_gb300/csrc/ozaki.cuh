@@ -119,7 +119,8 @@ __device__ __forceinline__ int scale_exp(float m) {
 }
 
 // Peels 8 scaled values (already multiplied by 2^(7 - e)) into up to S
-// slices; q[s][j] receives slice s of value j.
+// slices; q[s][j] receives slice s of value j.  (t - r) * 256 is exact, so one
+// fused multiply-add forms it.
 template <int S>
 __device__ __forceinline__ void peel8(float (&t)[8], float (&q)[S][8]) {
 #pragma unroll
@@ -128,18 +129,23 @@ __device__ __forceinline__ void peel8(float (&t)[8], float (&q)[S][8]) {
         for (int j = 0; j < 8; ++j) {
             const float r = rintf(t[j]);
             q[s][j] = r;
-            t[j] = (t[j] - r) * 256.0f;
+            t[j] = __fmaf_rn(t[j], 256.0f, -256.0f * r);
         }
 }
 
-__device__ __forceinline__ uint4 pack8(const float (&v)[8], float sign) {
+__device__ __forceinline__ uint4 pack8(const float (&v)[8]) {
     uint32_t w[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        __nv_bfloat162 h = __floats2bfloat162_rn(sign * v[2 * i], sign * v[2 * i + 1]);
+        __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
         w[i] = *reinterpret_cast<uint32_t *>(&h);
     }
     return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// The same eight bf16 values negated (sign bits flipped).
+__device__ __forceinline__ uint4 neg8(uint4 v) {
+    return make_uint4(v.x ^ 0x80008000u, v.y ^ 0x80008000u, v.z ^ 0x80008000u, v.w ^ 0x80008000u);
 }
 
 // Stores slices of 8 consecutive elements (row, k0..k0+7) of a real plane into
@@ -151,11 +157,12 @@ __device__ __forceinline__ void store_a8(unsigned char *sa, int row, int k0, int
 #pragma unroll
     for (int s = 0; s < S; ++s) {
         unsigned char *base = sa + s * kASlice;
+        const uint4 v = pack8(q[s]);
         if (plane == 0) {
-            *reinterpret_cast<uint4 *>(base + kBlk + off) = pack8(q[s], 1.0f);
+            *reinterpret_cast<uint4 *>(base + kBlk + off) = v;
         } else {
-            *reinterpret_cast<uint4 *>(base + 2 * kBlk + off) = pack8(q[s], 1.0f);
-            *reinterpret_cast<uint4 *>(base + off) = pack8(q[s], -1.0f);
+            *reinterpret_cast<uint4 *>(base + 2 * kBlk + off) = v;
+            *reinterpret_cast<uint4 *>(base + off) = neg8(v);
         }
     }
 }
@@ -166,7 +173,7 @@ template <int S>
 __device__ __forceinline__ void store_b8(unsigned char *sb, int n, int k0, int plane, const float (&q)[S][8]) {
     const uint32_t off = sw(n, k0) + (uint32_t)plane * kBlk;
 #pragma unroll
-    for (int s = 0; s < S; ++s) *reinterpret_cast<uint4 *>(sb + s * kBSlice + off) = pack8(q[s], 1.0f);
+    for (int s = 0; s < S; ++s) *reinterpret_cast<uint4 *>(sb + s * kBSlice + off) = pack8(q[s]);
 }
 
 }  // namespace oz

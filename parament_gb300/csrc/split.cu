@@ -442,9 +442,14 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
     const void *fn = pick_split(d);
     const size_t smem = split_smem(d, (int)c->Ke);
     cudaError_t e = cudaSuccess;
+    a.wts = nullptr;
     if (tensor) {
-        // One CTA per SM (tensor-core kernel).
+        // One CTA per SM (tensor-core kernel); the step weights go to a buffer
+        // of P x Ke double-float values first.
         a.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)c->num_sms, P));
+        if (c->wts.ensure(std::max<size_t>(16, sizeof(float4) * (size_t)P * c->Ke)) != cudaSuccess)
+            return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+        a.wts = static_cast<const float4 *>(c->wts.ptr);
     } else {
         e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0;

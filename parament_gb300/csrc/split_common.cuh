@@ -87,6 +87,7 @@ struct SplitArgs {
     unsigned pts;
     int K, amps, mode, magnus;
     double hfac;
+    const float4 *wts;                  // P x Ke step weights in double-float (re hi, re lo, im hi, im lo)
 };
 
 // Weight m of step s in FP64 from complex64 samples (src/cuda/control_expansion.cu:27-170,

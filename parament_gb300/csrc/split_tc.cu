@@ -25,14 +25,15 @@
 // Re C in tensor-memory lanes 0..63 and Im C in lanes 64..127, and each thread
 // keeps the plane of its own lane for 32 columns.  X Q = i X N comes from the
 // same slices with the A blocks swapped (ozaki.cuh).  Only the first-order
-// term mu_1 X = i nu_1 X couples the planes; it is formed in double-float by
-// the assembly, which computes whole complex elements and hands each partner
-// thread its plane through shared memory.
+// term mu_1 X = i nu_1 X couples the planes; the assembly leaves X_j in
+// double-float in shared memory and each thread forms its plane of mu_1 X from
+// the other plane there.
 //
 // Layout of one CTA (512 threads, one per SM): shared memory holds the A
-// slices (4 x 24 KB), the B slices (4 x 16 KB) and a 48 KB exchange buffer;
-// tensor memory holds the product levels (columns 0..255) and E^P in
-// double-float (columns 256..383).  Sixteen warps hide the latency of the
+// slices (4 x 24 KB) and the B slices (4 x 16 KB); during the assembly the
+// same 160 KB stage the expansion matrices (bulk copies, five at a time) and
+// then the planes that hand X_j to the lane layout.  Tensor memory holds the
+// product levels (columns 0..255) and E^P in double-float (columns 256..383).  Sixteen warps hide the latency of the
 // elementwise work (assembly, slicing, epilogues) that surrounds each
 // product; each thread owns one plane of 16 columns of one row.  Every wait on the tensor core is bounded:
 // a wait that runs out stops the CTA, counts a fault and frees tensor memory.
@@ -60,11 +61,33 @@ constexpr int kTcdG = 2;
 constexpr uint32_t kTcdWait = 1u << 24;
 constexpr size_t kTcdSA = (size_t)kTcdHi * oz::kASlice;
 constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
-constexpr int kTcdXch = 24;  // floats a thread hands its partner after the assembly
-constexpr size_t kTcdST = (size_t)kTcdXch * kTcdThreads * sizeof(float);
-constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdST + 1024;
+constexpr size_t kTcdSmem = kTcdSA + kTcdSB + 1024;
+// During the assembly the slice buffers are free: they take up to five
+// expansion matrices (32 KB each) at a time, streamed in by bulk copies.
+constexpr int kTcdStageMats = 5;
+constexpr uint32_t kTcdMatBytes = 64 * 64 * 8;
+static_assert(kTcdStageMats * kTcdMatBytes <= kTcdSA + kTcdSB, "staging exceeds the slice buffers");
+// After the assembly X_j passes to the lane layout through four planes of
+// 64 rows padded to 68 floats (conflict-free 16-byte reads of a column block
+// by 32 consecutive rows), also over the slice buffers.
+constexpr int kTcdPlaneLd = 68;
+constexpr int kTcdPlane = 64 * kTcdPlaneLd;
+static_assert(4 * kTcdPlane * sizeof(float) <= kTcdSA + kTcdSB, "planes exceed the slice buffers");
 
 __device__ int g_split_tc_faults;
+
+// Bulk copy global -> shared memory completing on an mbarrier (transaction
+// count), and the arrival that announces the bytes to expect.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     tc::smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(tc::smem_addr(bar))
+                 : "memory");
+}
 
 // TMEM <- registers, 32 lanes x 16 columns (one warp).
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
@@ -109,7 +132,7 @@ __device__ __forceinline__ void peel8_df(const float (&hi)[8], const float (&lo)
         for (int s = 1; s < S; ++s) {
             const float r = rintf(t);
             q[s][j] = r;
-            t = (t - r) * 256.0f;
+            t = __fmaf_rn(t, 256.0f, -256.0f * r);
         }
     }
 }
@@ -118,7 +141,8 @@ struct TcdShared {
     float4 ws[2][kTcdMaxKe];       // step weights (double-float re, im), double-buffered across steps
     int amax[2][64], bmax[2][64];
     float rowmul[64], colmul[64];  // 2^(e - 7) of the last A rows / B columns
-    uint64_t bar;
+    uint64_t bar;                  // tensor-core products
+    uint64_t tbar;                 // bulk copies of the expansion matrices
     uint32_t tmem_base;
 };
 
@@ -219,7 +243,7 @@ __device__ __forceinline__ void store_b(TcdShared &sh, unsigned char *SB, const 
         }
         const uint32_t off = oz::sw(k, t.c0 + 8 * g);
 #pragma unroll
-        for (int s = 0; s < S; ++s) *reinterpret_cast<uint4 *>(SB + s * oz::kBSlice + off) = oz::pack8(q[s], 1.0f);
+        for (int s = 0; s < S; ++s) *reinterpret_cast<uint4 *>(SB + s * oz::kBSlice + off) = oz::pack8(q[s]);
     }
 }
 
@@ -363,7 +387,6 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     unsigned char *SA = smem;
     unsigned char *SB = smem + kTcdSA;
-    float *ST = reinterpret_cast<float *>(SB + kTcdSB);
     __shared__ TcdShared sh;
 
     const int warp = threadIdx.x >> 5;
@@ -385,6 +408,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     }
     if (t.tid == 0) {
         tc::mbar_init(&sh.bar, 1);
+        tc::mbar_init(&sh.tbar, 1);
         tc::fence_mbar_init();
     }
     if (t.tid < 64) {
@@ -406,117 +430,149 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     uint32_t ncommit = 0;
     int nb = 0;  // max-buffer parity
     bool ok = true;
-    // Step weights are computed one step ahead by the first Ke threads, so
-    // their sample loads overlap the previous step's products.
-    auto weights = [&](long long st, int buf) {
-        for (int m = t.tid; m < a.Ke; m += blockDim.x) {
-            const double2 w = split_weight(a, m, st);
-            const df re = df_from(w.x), im = df_from(w.y);
-            sh.ws[buf][m] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    // Expansion matrices H_0 .. H_Ke reach shared memory in rounds of up to
+    // kTcdStageMats bulk copies; round 0 of the next step is issued as soon
+    // as the tensor core is done with the slice buffers.
+    const int nmat = a.Ke + 1;
+    const int nrounds = (nmat + kTcdStageMats - 1) / kTcdStageMats;
+    uint32_t tphase = 0, tissued = 0;  // rounds waited for / issued (same in every thread)
+    auto issue_round = [&](int r) {
+        ++tissued;
+        if (t.tid == 0) {
+            const int n = min(kTcdStageMats, nmat - r * kTcdStageMats);
+            mbar_expect_tx(&sh.tbar, n * kTcdMatBytes);
+            for (int i = 0; i < n; ++i)
+                bulk_g2s(SA + i * kTcdMatBytes, a.stack + (size_t)(r * kTcdStageMats + i) * 4096, kTcdMatBytes, &sh.tbar);
         }
     };
-    if (s1 > s0) weights(s0, 0);
+    // Step weights (k_split_weights) reach shared memory one step ahead.
+    if (t.tid < a.Ke && s1 > s0) sh.ws[0][t.tid] = a.wts[(size_t)s0 * a.Ke + t.tid];
+    if (s1 > s0) issue_round(0);
     __syncthreads();
     for (long long st = s0; st < s1; ++st) {
         const int wb = (int)((st - s0) & 1);
-        // ---- assembly: whole complex elements of row r, columns cm .. cm + 7
+        float4 wnext = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (t.tid < a.Ke && st + 1 < s1) wnext = a.wts[(size_t)(st + 1) * a.Ke + t.tid];
+        // ---- assembly.  Coalesced mapping: thread tid forms the complex
+        // pairs held by float4 f = 512 j + tid of a matrix (row f / 32,
+        // columns 2 (f % 32), + 1), j = 0..3, so that every warp reads 512
+        // contiguous bytes of each staged matrix.
         float X[16], Eh[16], El[16];
         {
-            const int cm = t.c0 + 8 * t.p;
-            const size_t e0 = (size_t)t.r * 64 + cm;
             float xrh[8], xrl[8], xih[8], xil[8], sr[8], si[8];
-            {
-                const float4 *H0 = reinterpret_cast<const float4 *>(a.stack + e0);
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const float4 v = H0[j];
-                    xrh[2 * j] = v.x;
-                    xih[2 * j] = v.y;
-                    xrh[2 * j + 1] = v.z;
-                    xih[2 * j + 1] = v.w;
+            for (int j = 0; j < 8; ++j) xrl[j] = xil[j] = sr[j] = si[j] = 0.0f;
+            for (int rd = 0; rd < nrounds; ++rd) {
+                if (rd > 0) {
+                    // Every thread is done with the previous round's matrices.
+                    tc::fence_proxy_async();
+                    __syncthreads();
+                    issue_round(rd);
                 }
+                ok = tc::mbar_wait(&sh.tbar, tphase & 1, kTcdWait) && ok;
+                ++tphase;
+                const int mb = rd * kTcdStageMats, me = min(nmat, mb + kTcdStageMats);
+                for (int mm = mb; mm < me; ++mm) {
+                    const float4 *Hm = reinterpret_cast<const float4 *>(SA + (mm - mb) * kTcdMatBytes) + t.tid;
+                    float gr[8], gi[8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) xrl[j] = xil[j] = sr[j] = si[j] = 0.0f;
-            }
-            for (int m = 0; m < a.Ke; ++m) {
-                const float4 *Hm = reinterpret_cast<const float4 *>(a.stack + (size_t)(m + 1) * 4096 + e0);
-                const float4 w = sh.ws[wb][m];
-                float gr[8], gi[8];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const float4 v = Hm[j];
-                    gr[2 * j] = v.x;
-                    gi[2 * j] = v.y;
-                    gr[2 * j + 1] = v.z;
-                    gi[2 * j + 1] = v.w;
-                }
-                // The branches depend on the slot's weight only: uniform over the CTA.
-                if (m < a.K) {
-                    if (w.z == 0.0f && w.w == 0.0f) {  // real weight (real control samples)
+                    for (int j = 0; j < 4; ++j) {
+                        const float4 v = Hm[512 * j];
+                        gr[2 * j] = v.x;
+                        gi[2 * j] = v.y;
+                        gr[2 * j + 1] = v.z;
+                        gi[2 * j + 1] = v.w;
+                    }
+                    if (mm == 0) {
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
-                            df_mac_lazy(xrh[j], xrl[j], w.x, w.y, gr[j]);
-                            df_mac_lazy(xih[j], xil[j], w.x, w.y, gi[j]);
+                            xrh[j] = gr[j];
+                            xih[j] = gi[j];
+                        }
+                        continue;
+                    }
+                    const int m = mm - 1;
+                    const float4 w = sh.ws[wb][m];
+                    // The branches depend on the slot's weight only: uniform over the CTA.
+                    if (m < a.K) {
+                        if (w.z == 0.0f && w.w == 0.0f) {  // real weight (real control samples)
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                df_mac_lazy(xrh[j], xrl[j], w.x, w.y, gr[j]);
+                                df_mac_lazy(xih[j], xil[j], w.x, w.y, gi[j]);
+                            }
+                        } else {
+                            const cdf wd = {{w.x, w.y}, {w.z, w.w}};
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                const cdf x = cdf_add(cdf{df_norm(xrh[j], xrl[j]), df_norm(xih[j], xil[j])},
+                                                      cdf_mul_c(wd, make_float2(gr[j], gi[j])));
+                                xrh[j] = x.re.hi;
+                                xrl[j] = x.re.lo;
+                                xih[j] = x.im.hi;
+                                xil[j] = x.im.lo;
+                            }
+                        }
+                    } else if (w.x == 0.0f) {
+                        // commutator slot with an imaginary weight i v: w h = -v h_i + i v h_r
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            sr[j] = fmaf(-w.z, gi[j], sr[j]);
+                            si[j] = fmaf(w.z, gr[j], si[j]);
                         }
                     } else {
-                        const cdf wd = {{w.x, w.y}, {w.z, w.w}};
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
-                            const cdf x = cdf_add(cdf{df_norm(xrh[j], xrl[j]), df_norm(xih[j], xil[j])},
-                                                  cdf_mul_c(wd, make_float2(gr[j], gi[j])));
-                            xrh[j] = x.re.hi;
-                            xrl[j] = x.re.lo;
-                            xih[j] = x.im.hi;
-                            xil[j] = x.im.lo;
+                            sr[j] = fmaf(w.x, gr[j], fmaf(-w.z, gi[j], sr[j]));
+                            si[j] = fmaf(w.x, gi[j], fmaf(w.z, gr[j], si[j]));
                         }
-                    }
-                } else if (w.x == 0.0f) {
-                    // commutator slot with an imaginary weight i v: w h = -v h_i + i v h_r
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        sr[j] = fmaf(-w.z, gi[j], sr[j]);
-                        si[j] = fmaf(w.z, gr[j], si[j]);
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        sr[j] = fmaf(w.x, gr[j], fmaf(-w.z, gi[j], sr[j]));
-                        si[j] = fmaf(w.x, gi[j], fmaf(w.z, gr[j], si[j]));
                     }
                 }
             }
-            // E = c0 I + i nu_1 X; keep plane p, send plane 1 - p to the partner (tid ^ 64).
-            float mx[8], meh[8], mel[8];
+            // X in double-float into four row-padded planes (re hi, re lo, im hi,
+            // im lo) over the staging buffers, then read back in the lane layout.
+            tc::fence_proxy_async();
+            __syncthreads();
+            float *XP = reinterpret_cast<float *>(SA);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const df xr = df_add_f(df_norm(xrh[j], xrl[j]), sr[j]);
-                const df xi = df_add_f(df_norm(xih[j], xil[j]), si[j]);
-                df er = df_neg(df_mul(nu1, xi));
-                if (t.r == cm + j) er = df_add(er, c0d);
-                const df ei = df_mul(nu1, xr);
-                const df mine = t.p ? ei : er, other = t.p ? er : ei;
-                mx[j] = t.p ? xi.hi : xr.hi;
-                meh[j] = mine.hi;
-                mel[j] = mine.lo;
-                ST[j * kTcdThreads + t.tid] = t.p ? xr.hi : xi.hi;
-                ST[(8 + j) * kTcdThreads + t.tid] = other.hi;
-                ST[(16 + j) * kTcdThreads + t.tid] = other.lo;
+            for (int j = 0; j < 4; ++j) {
+                const int f = 512 * j + t.tid, row = f >> 5, col = 2 * (f & 31);
+                const df r0 = df_add_f(df_norm(xrh[2 * j], xrl[2 * j]), sr[2 * j]);
+                const df r1 = df_add_f(df_norm(xrh[2 * j + 1], xrl[2 * j + 1]), sr[2 * j + 1]);
+                const df i0 = df_add_f(df_norm(xih[2 * j], xil[2 * j]), si[2 * j]);
+                const df i1 = df_add_f(df_norm(xih[2 * j + 1], xil[2 * j + 1]), si[2 * j + 1]);
+                const int o = row * kTcdPlaneLd + col;
+                *reinterpret_cast<float2 *>(XP + o) = make_float2(r0.hi, r1.hi);
+                *reinterpret_cast<float2 *>(XP + kTcdPlane + o) = make_float2(r0.lo, r1.lo);
+                *reinterpret_cast<float2 *>(XP + 2 * kTcdPlane + o) = make_float2(i0.hi, i1.hi);
+                *reinterpret_cast<float2 *>(XP + 3 * kTcdPlane + o) = make_float2(i0.lo, i1.lo);
             }
             __syncthreads();
             // The next step's weights: every thread is past this step's assembly.
-            if (st + 1 < s1) weights(st + 1, wb ^ 1);
-            // Own half at columns 8 p .., the partner's at 8 (1 - p) ..
-            const int partner = t.tid ^ 64;
+            if (t.tid < a.Ke) sh.ws[wb ^ 1][t.tid] = wnext;
+            // E = c0 I + i nu_1 X in this thread's plane: E_re = c0 d - nu_1 X_im,
+            // E_im = nu_1 X_re.
+            {
+                const float4 *own = reinterpret_cast<const float4 *>(XP + 2 * t.p * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
+                const float4 *oh = reinterpret_cast<const float4 *>(XP + 2 * (1 - t.p) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
+                const float4 *ol = reinterpret_cast<const float4 *>(XP + (2 * (1 - t.p) + 1) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const float rx = ST[j * kTcdThreads + partner], reh = ST[(8 + j) * kTcdThreads + partner],
-                            rel = ST[(16 + j) * kTcdThreads + partner];
-                X[j] = t.p ? rx : mx[j];
-                X[8 + j] = t.p ? mx[j] : rx;
-                Eh[j] = t.p ? reh : meh[j];
-                Eh[8 + j] = t.p ? meh[j] : reh;
-                El[j] = t.p ? rel : mel[j];
-                El[8 + j] = t.p ? mel[j] : rel;
+                for (int g = 0; g < 4; ++g) {
+                    const float4 x = own[g], h = oh[g], l = ol[g];
+                    const float xs[4] = {x.x, x.y, x.z, x.w}, hs[4] = {h.x, h.y, h.z, h.w}, ls[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int j = 4 * g + i;
+                        X[j] = xs[i];
+                        df e = df_mul(nu1, df{hs[i], ls[i]});
+                        if (t.p == 0) {
+                            e = df_neg(e);
+                            if (t.c0 + j == t.r) e = df_add(e, c0d);
+                        }
+                        Eh[j] = e.hi;
+                        El[j] = e.lo;
+                    }
+                }
             }
         }
         // ---- X^2
@@ -575,6 +631,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         }
         // ---- running product E^P <- E^P + E + E E^P
         if (st == s0) {
+            if (st + 1 < s1) issue_round(0);  // the slice buffers are free again
             store_ep(t.tm_ep, Eh, El);
         } else {
             {
@@ -586,6 +643,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             store_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
             nb ^= 1;
             if (!run_product(sh, t, SA, SB, kTcdHi, kTcdHi, kTcdHi - 1, false, ncommit, ok)) break;
+            if (st + 1 < s1) issue_round(0);  // the slice buffers are free again
             epilogue_running(sh, t, Eh, El);
         }
     }
@@ -606,14 +664,29 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     }
     if (!ok) {
         if (t.tid == 0) atomicAdd(&g_split_tc_faults, 1);
-        // Let any product still in flight finish before tensor memory is released.
-        tc::mbar_wait(&sh.bar, (ncommit - 1) & 1, kTcdWait);
+        // Let any product or copy still in flight finish before tensor memory
+        // and shared memory are released.
+        if (ncommit > 0) tc::mbar_wait(&sh.bar, (ncommit - 1) & 1, kTcdWait);
     }
+    for (; tphase < tissued; ++tphase) tc::mbar_wait(&sh.tbar, tphase & 1, kTcdWait);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
         tc::fence_after_sync();
         tc::tmem_dealloc(sh.tmem_base, 512);
+    }
+}
+
+// Step weights of the split form in double-float for all steps (the step
+// kernel reads them one step ahead): weight m of step s at wts[s Ke + m].
+__global__ void k_split_weights(const __grid_constant__ SplitArgs a, float4 *wts) {
+    const long long n = a.P * a.Ke;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long st = i / a.Ke;
+        const int m = (int)(i - st * a.Ke);
+        const double2 w = split_weight(a, m, st);
+        const df re = df_from(w.x), im = df_from(w.y);
+        wts[i] = make_float4(re.hi, re.lo, im.hi, im.lo);
     }
 }
 
@@ -633,6 +706,12 @@ cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, int *nchunks, cudaS
     cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_split_tc),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcdSmem);
     if (e != cudaSuccess) return e;
+    if (a.Ke > 0) {
+        const long long n = a.P * a.Ke;
+        const int blocks = (int)std::min<long long>((n + 255) / 256, 8L * num_sms);
+        k_split_weights<<<blocks, 256, 0, stream>>>(a, const_cast<float4 *>(a.wts));
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     SplitArgs b = a;
     b.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)num_sms, a.P));
     *nchunks = b.nchunks;
