@@ -381,6 +381,39 @@ __device__ __forceinline__ void df_mac_lazy(float &hi, float &lo, float wh, floa
     lo = __fadd_rn(lo, __fadd_rn(t, e));
 }
 
+// The same on two values at once with the paired FP32 instructions of
+// sm_100-family GPUs (add/mul/fma.rn.f32x2: each half rounds exactly as the
+// scalar instruction): (hi, lo)[k] += w h[k], k = 0, 1 (the real and
+// imaginary parts of one element, which share the weight).
+__device__ __forceinline__ void df_mac_lazy2(float &hi0, float &hi1, float &lo0, float &lo1, float wh, float wl,
+                                             float h0, float h1) {
+    asm("{\n\t"
+        ".reg .b64 H, L, W, N, V, X, P, E, S, B, T, U;\n\t"
+        "mov.b64 H, {%0, %1};\n\t"
+        "mov.b64 L, {%2, %3};\n\t"
+        "mov.b64 W, {%4, %4};\n\t"
+        "mov.b64 N, {%8, %8};\n\t"
+        "mov.b64 V, {%5, %5};\n\t"
+        "mov.b64 X, {%6, %7};\n\t"
+        "mul.rn.f32x2 P, W, X;\n\t"       // p = wh h
+        "mul.rn.f32x2 E, N, X;\n\t"       // -p
+        "fma.rn.f32x2 E, W, X, E;\n\t"    // e = wh h - p (exact)
+        "fma.rn.f32x2 E, V, X, E;\n\t"    // e += wl h
+        "add.rn.f32x2 S, H, P;\n\t"       // two_sum(hi, p): s
+        "sub.rn.f32x2 B, S, H;\n\t"       // bb = s - hi
+        "sub.rn.f32x2 T, S, B;\n\t"
+        "sub.rn.f32x2 T, H, T;\n\t"       // hi - (s - bb)
+        "sub.rn.f32x2 U, P, B;\n\t"       // p - bb
+        "add.rn.f32x2 T, T, U;\n\t"       // t
+        "add.rn.f32x2 T, T, E;\n\t"
+        "add.rn.f32x2 L, L, T;\n\t"       // lo += t + e
+        "mov.b64 {%0, %1}, S;\n\t"
+        "mov.b64 {%2, %3}, L;\n\t"
+        "}"
+        : "+f"(hi0), "+f"(hi1), "+f"(lo0), "+f"(lo1)
+        : "f"(wh), "f"(wl), "f"(h0), "f"(h1), "f"(-wh));
+}
+
 __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_constant__ SplitArgs a) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem =
@@ -497,10 +530,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                     if (m < a.K) {
                         if (w.z == 0.0f && w.w == 0.0f) {  // real weight (real control samples)
 #pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                df_mac_lazy(xrh[j], xrl[j], w.x, w.y, gr[j]);
-                                df_mac_lazy(xih[j], xil[j], w.x, w.y, gi[j]);
-                            }
+                            for (int j = 0; j < 8; ++j)
+                                df_mac_lazy2(xrh[j], xih[j], xrl[j], xil[j], w.x, w.y, gr[j], gi[j]);
                         } else {
                             const cdf wd = {{w.x, w.y}, {w.z, w.w}};
 #pragma unroll
