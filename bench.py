@@ -339,10 +339,11 @@ def ensemble_block(torch, parament, K_steps, W_steps):
     return out
 
 
-def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, steps=1024):
+def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, steps=1024, err_steps=256):
     """Large dense workload, complex64 d=512, K=8, ||H0|| = 20, smooth
     8-mode Fourier controls, on a 1024-step prefix of the 8192 steps: the
-    tcgen05 3xTF32 GEMM path (kernel k_tc_cgemm)."""
+    tcgen05 3xTF32 GEMM path (kernel k_tc_cgemm).  The error column compares
+    the complex64 result with the complex128 one on a 256-step prefix."""
     from parament_gb300 import workloads
     w = workloads.large_dense(d=512, K=8, steps=steps)
     ctx = parament.Parament("fp32")
@@ -366,9 +367,50 @@ def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, steps=10
     M = ctx.last_iteration_cycles
     ctx.destroy()
     flops = steps * (M + 1) * 8.0 * 512 ** 3
+    # complex64 against complex128 on the same (complex64-rounded) inputs
+    we = workloads.large_dense(d=512, K=8, steps=err_steps)
+    H0, H1, ce = (we[k].astype(np.complex64).astype(np.complex128) for k in ("H0", "H1", "carr"))
+    Us = []
+    for prec in ("fp32", "fp64"):
+        with parament.Parament(prec) as c:
+            c.set_hamiltonian(H0, *H1)
+            Us.append(c.equiprop(we["dt"], *ce).astype(np.complex128))
+    err = float(np.linalg.norm(Us[0] - Us[1]) / np.linalg.norm(Us[1]))
     return {"workload": f"large_dense d=512 K=8 complex64, first {steps} steps", "M": M, "ms": round(ms, 3),
             "steps_per_s": round(steps / (ms * 1e-3), 1), "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
-            "kernel": "k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)"}
+            "kernel": "k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)",
+            "rel_err_vs_fp64": err, "rel_err_steps": err_steps,
+            "scheme": "the reference's plain complex64 scheme (fp32 order table)"}
+
+
+def large_dense_c128_block(torch, parament, K_steps, W_steps, stream, steps=4):
+    """Large dense complex128 workload, d=1024, K=4, ||H0|| = 20: the first
+    `steps` of its 2048 steps on the FP64 GEMM path (k_gemm, FP64 pipe)."""
+    from parament_gb300 import workloads
+    w = workloads.large_dense(d=1024, K=4, steps=steps)
+    ctx = parament.Parament("fp64")
+    ctx.set_hamiltonian(w["H0"], *w["H1"])
+    carr = torch.tensor(w["carr"], dtype=torch.complex128, device="cuda")
+    out = torch.empty((1024, 1024), dtype=torch.complex128, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(W_steps):
+            ctx.equiprop_device(w["dt"], carr, out, stream)
+        stream.synchronize()
+        ts = []
+        for _ in range(K_steps):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            ctx.equiprop_device(w["dt"], carr, out, stream)
+            e.record(stream)
+            ts.append((s, e))
+        stream.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ts) / len(ts)
+    M = ctx.last_iteration_cycles
+    ctx.destroy()
+    flops = steps * (M + 1) * 8.0 * 1024 ** 3
+    return {"workload": f"large_dense d=1024 K=4 complex128, first {steps} of 2048 steps", "M": M,
+            "ms": round(ms, 3), "steps_per_s": round(steps / (ms * 1e-3), 2),
+            "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 3), "kernel": "k_gemm (FP64 pipe)"}
 
 
 def cpu_baseline(w, target_s=10.0):
@@ -566,6 +608,10 @@ def run_ours(args, rank, world, local):
         line["large_dense"] = large_dense_block(torch, parament, args.steps, args.warmup, flush, stream)
     except (ValueError, RuntimeError) as e:
         line["large_dense"] = {"error": str(e)}
+    try:
+        line["large_dense_c128"] = large_dense_c128_block(torch, parament, min(args.steps, 2), 1, stream)
+    except (ValueError, RuntimeError) as e:
+        line["large_dense_c128"] = {"error": str(e)}
     if not args.no_ensemble:
         try:
             line["ensemble"] = ensemble_block(torch, parament, args.steps, args.warmup)

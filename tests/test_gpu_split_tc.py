@@ -97,3 +97,39 @@ def test_repeated_calls_agree(built_lib):
     U1, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
     U2, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
     assert np.array_equal(U1, U2)
+
+
+def test_fewer_sample_arrays_than_controls(built_lib):
+    """Magnus with 4 controls loaded and 2 sample arrays: the rest are zero."""
+    H0, H1, carr = problem(4, 2 * 300 + 1, seed=31)
+    U, _ = split_equiprop(H0, H1, list(carr[:2]), 1e-3, True, oracle.SIMPSON)
+    full = np.concatenate([carr[:2], np.zeros_like(carr[2:])])
+    Uo = oracle.equiprop(H0, H1, full, 1e-3, magnus=True, mode=oracle.SIMPSON, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
+
+
+def test_matches_simt_split_kernel(built_lib):
+    """The tensor-core kernel and the SIMT split kernel (tensor cores disabled
+    through PARAMENT_DISABLE_TENSOR_CORES in a child process) agree within the
+    split form's bar, on the d=64 Magnus workload at 4096 steps."""
+    import subprocess
+    import sys
+    import tempfile
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys, numpy as np, parament_gb300 as p\n"
+            "from parament_gb300 import workloads\n"
+            "w = workloads.magnus_d64(4096)\n"
+            "c = lambda x: x.astype(np.complex64)\n"
+            "ctx = p.Parament('fp32'); ctx.set_precision_mode('split')\n"
+            "ctx.set_hamiltonian(c(w['H0']), *c(w['H1']), use_magnus=True, quadrature_mode='simpson')\n"
+            "np.save(sys.argv[1], ctx.equiprop(w['dt'], *c(w['carr'])))\n")
+    outs = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for tag, env in (("tc", {}), ("simt", {"PARAMENT_DISABLE_TENSOR_CORES": "1"})):
+            f = os.path.join(tmp, tag + ".npy")
+            r = subprocess.run([sys.executable, "-c", code, f], cwd=root, env=dict(os.environ, **env),
+                               capture_output=True, text=True, timeout=600)
+            assert r.returncode == 0, r.stderr
+            outs.append(np.load(f).astype(np.complex128))
+    assert relerr(outs[0], outs[1]) < TOL
+    assert not np.array_equal(outs[0], outs[1])  # two different kernels ran
