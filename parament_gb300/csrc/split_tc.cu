@@ -33,10 +33,12 @@
 // slices (4 x 24 KB) and the B slices (4 x 16 KB); during the assembly the
 // same 160 KB stage the expansion matrices (bulk copies, five at a time) and
 // then the planes that hand X_j to the lane layout.  Tensor memory holds the
-// product levels (columns 0..255) and E^P in double-float (columns 256..383).  Sixteen warps hide the latency of the
-// elementwise work (assembly, slicing, epilogues) that surrounds each
-// product; each thread owns one plane of 16 columns of one row.  Every wait on the tensor core is bounded:
-// a wait that runs out stops the CTA, counts a fault and frees tensor memory.
+// product levels (columns 0..255), E^P in double-float (256..383) and E of
+// the current step (384..511) while the polynomial products run.  Sixteen
+// warps hide the latency of the elementwise work (assembly, slicing,
+// epilogues) that surrounds each product; each thread owns one plane of 16
+// columns of one row.  Every wait on the tensor core is bounded: a wait that
+// runs out stops the CTA, counts a fault and frees tensor memory.
 #include <math.h>
 #include <stdlib.h>
 
@@ -152,7 +154,7 @@ struct TcdShared {
 // c0 = 16 (w / 4).  Warps w and w ^ 2 hold the two planes of the same elements.
 struct TcdThread {
     int tid, lane, p, r, c0, cb;
-    uint32_t tm_acc, tm_ep;
+    uint32_t tm_acc, tm_ep, tm_e;
 };
 
 // Operand slicing.  reduce_max() posts this thread's row maximum of the A
@@ -454,6 +456,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     const uint32_t lane_base = (uint32_t)(32 * q4) << 16;
     t.tm_acc = sh.tmem_base + lane_base + (uint32_t)t.c0;
     t.tm_ep = sh.tmem_base + lane_base + 256u + 32u * (uint32_t)t.cb;
+    t.tm_e = sh.tmem_base + lane_base + 384u + 32u * (uint32_t)t.cb;
 
     // Coefficients: c0 = m_0 - 1 and even mu real, odd mu = i nu.
     const df nu1 = df_from(a.mu[1].y);
@@ -490,7 +493,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         // pairs held by float4 f = 512 j + tid of a matrix (row f / 32,
         // columns 2 (f % 32), + 1), j = 0..3, so that every warp reads 512
         // contiguous bytes of each staged matrix.
-        float X[16], Eh[16], El[16];
+        float X[16];
         {
             float xrh[8], xrl[8], xih[8], xil[8], sr[8], si[8];
 #pragma unroll
@@ -584,6 +587,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             // E = c0 I + i nu_1 X in this thread's plane: E_re = c0 d - nu_1 X_im,
             // E_im = nu_1 X_re.
             {
+                float Eh[16], El[16];
                 const float4 *own = reinterpret_cast<const float4 *>(XP + 2 * t.p * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
                 const float4 *oh = reinterpret_cast<const float4 *>(XP + 2 * (1 - t.p) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
                 const float4 *ol = reinterpret_cast<const float4 *>(XP + (2 * (1 - t.p) + 1) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
@@ -604,6 +608,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                         El[j] = e.lo;
                     }
                 }
+                // E waits in tensor memory while the polynomial products run.
+                store_ep(t.tm_e, Eh, El);
             }
         }
         // ---- X^2
@@ -616,6 +622,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         epilogue_f<kTcdX2 - 1>(sh, t, G);
         {
             const float nu3 = (float)a.mu[3].y;
+            float Eh[16], El[16];
+            load_ep(t.tm_e, Eh, El);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const df v = df_add(df{Eh[j], El[j]}, df_mul_f(mu2, G[j]));
@@ -623,6 +631,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                 El[j] = v.lo;
                 N[j] = nu3 * G[j];
             }
+            store_ep(t.tm_e, Eh, El);
         }
         // ---- higher even powers X^(2k) = X^(2k-2) X^2
         bool live = true;
@@ -638,6 +647,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             epilogue_f<kTcdG - 1>(sh, t, G);
             const float me = (float)a.mu[2 * k].x;
             const float no = (2 * k + 1 <= M) ? (float)a.mu[2 * k + 1].y : 0.0f;
+            float Eh[16], El[16];
+            load_ep(t.tm_e, Eh, El);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const df v = df_add_f(df{Eh[j], El[j]}, me * G[j]);
@@ -645,6 +656,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                 El[j] = v.lo;
                 N[j] = fmaf(no, G[j], N[j]);
             }
+            store_ep(t.tm_e, Eh, El);
         }
         if (!live) break;
         // ---- odd part X Q = i X N
@@ -654,6 +666,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         nb ^= 1;
         if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, true, ncommit, ok)) break;
         epilogue_f<kTcdX2 - 1>(sh, t, G);
+        float Eh[16], El[16];
+        load_ep(t.tm_e, Eh, El);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             const df v = df_add_f(df{Eh[j], El[j]}, G[j]);
