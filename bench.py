@@ -57,17 +57,42 @@ def parse():
 
 
 def dist_init(n):
+    """Rank, world size and local rank from the torchrun environment; for N > 1
+    one process per GPU joins an NCCL group (gloo where no GPU is visible, so
+    that the replica logic runs on CPU too)."""
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
     elif torch.cuda.is_available():
         torch.cuda.set_device(0)
     return rank, world, local
+
+
+def max_over_ranks(x, world):
+    """The maximum over all ranks of a per-rank number (the slowest replica
+    sets the job's time)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, ms_per_step, world):
+    """Whole-job throughput of `world` replicas that each process
+    `units_per_rank` units in `ms_per_step` (the maximum over ranks)."""
+    return world * units_per_rank / (ms_per_step * 1e-3)
 
 
 class ClockSampler:
@@ -543,13 +568,9 @@ def run_ours(args, rank, world, local):
             torch.distributed.barrier()
         t_dev = [s.elapsed_time(e) for s, e in evs]
         ctx.destroy()
-    total_ms = sum(t_dev)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(t_dev), world)
     ms_per = total_ms / args.steps
-    value = world * P / (ms_per * 1e-3)
+    value = replica_value(P, ms_per, world)
     if rank != 0:
         return
 
