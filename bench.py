@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--profile-case", default=None,
-                   choices=["split_c64", "plain_c64", "plain_c128", "large_dense_d512", "vjp_d32"],
+                   choices=["split_c64", "plain_c64", "plain_c128", "large_dense_d512", "vjp_d32", "ensemble"],
                    help="run one form twice (for ncu captures) and exit")
     p.add_argument("--forms", default="plain_c128,plain_c64,split_c64",
                    help="comma-separated forms to measure (plain_c128 is the error reference)")
@@ -656,6 +656,18 @@ def profile_case(args):
     import parament_gb300 as parament
     from parament_gb300 import workloads
     case = args.profile_case
+    if case == "ensemble":
+        # The first 256 problems of the ensemble workload, run twice.
+        from parament_gb300.ensemble import Ensemble
+        probs = workloads.ensemble()[:256]
+        ens = Ensemble([(H0, H1, dt, c.shape[1]) for H0, H1, dt, c in probs], "fp32")
+        ens.set_samples([c for *_, c in probs])
+        for _ in range(2):
+            ens.run(copy_out=False)
+        torch.cuda.synchronize()
+        ens.destroy()
+        print("profile case", case, "done")
+        return
     if case == "large_dense_d512":
         w = workloads.large_dense(d=512, K=8, steps=32)
         ctx = parament.Parament("fp32")
