@@ -93,12 +93,17 @@ __device__ __forceinline__ void sts128(uint32_t a, float4 v) {
     asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
                  : "memory");
 }
+// Round to TF32 (10 explicit mantissa bits), nearest with ties away from zero,
+// by integer operations on the bits: half an ulp of TF32 is added to the
+// magnitude and the 13 low bits are cleared (a carry moves into the exponent).
+__device__ __forceinline__ float tf32_rna(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
 // x = hi + lo with hi, lo TF32; stores hi at hi_addr and lo at lo_addr.
 __device__ __forceinline__ void put_split4(uint32_t hi_addr, uint32_t lo_addr, float4 x) {
-    const float4 h = make_float4(tc::to_tf32(x.x), tc::to_tf32(x.y), tc::to_tf32(x.z), tc::to_tf32(x.w));
+    const float4 h = make_float4(tf32_rna(x.x), tf32_rna(x.y), tf32_rna(x.z), tf32_rna(x.w));
     sts128(hi_addr, h);
-    sts128(lo_addr, make_float4(tc::to_tf32(x.x - h.x), tc::to_tf32(x.y - h.y), tc::to_tf32(x.z - h.z),
-                                tc::to_tf32(x.w - h.w)));
+    sts128(lo_addr, make_float4(tf32_rna(x.x - h.x), tf32_rna(x.y - h.y), tf32_rna(x.z - h.z), tf32_rna(x.w - h.w)));
 }
 
 __device__ __forceinline__ void tc_arrive(uint64_t *bar) {
@@ -252,11 +257,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
             }
             tc::fence_before_sync();
             conv_sync();
-            // Second half: rows of the tile, 16 bytes (two complex) per thread.
+            // Second half: rows of the tile, 16 bytes (two complex) per thread;
+            // the sixteen Cin loads are all in flight before the first use.
             {
                 const float2 *Cin = g.Cin ? g.Cin + (size_t)b * g.sCin : nullptr;
                 float2 *Co = g.Cout + (size_t)b * g.sCout;
-#pragma unroll 4
+                float4 ci[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int idx = tid + 256 * i, rl = idx >> 5, c4 = idx & 31;
+                    ci[i] = Cin ? *reinterpret_cast<const float4 *>(Cin + (size_t)(r0 + rl) * d + c0 + 2 * c4)
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const int idx = tid + 256 * i, rl = idx >> 5, c4 = idx & 31;
                     const float4 v = lds128(stg_a + rl * kTcStagePitch + 16 * c4);
@@ -265,11 +278,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
                     float4 o = make_float4(g.alpha.x * v.x - g.alpha.y * v.y, g.alpha.x * v.y + g.alpha.y * v.x,
                                            g.alpha.x * v.z - g.alpha.y * v.w, g.alpha.x * v.w + g.alpha.y * v.z);
                     if (Cin) {
-                        const float4 ci = *reinterpret_cast<const float4 *>(Cin + e);
-                        o.x += g.beta * ci.x;
-                        o.y += g.beta * ci.y;
-                        o.z += g.beta * ci.z;
-                        o.w += g.beta * ci.w;
+                        o.x += g.beta * ci[i].x;
+                        o.y += g.beta * ci[i].y;
+                        o.z += g.beta * ci[i].z;
+                        o.w += g.beta * ci[i].w;
                     }
                     if (row == col) o.x += g.diag.x, o.y += g.diag.y;
                     if (row == col + 1) o.z += g.diag.x, o.w += g.diag.y;
