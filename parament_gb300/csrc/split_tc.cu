@@ -91,20 +91,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  : "memory");
 }
 
-// TMEM <- registers, 32 lanes x 16 columns (one warp).
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-            taddr),
-        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
-        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-        "r"(__float_as_uint(v[15]))
-        : "memory");
-}
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Column maxima of a warp: v[j] holds this lane's value of column j; on
 // return v[0] holds the maximum over the 32 lanes of column lane % 16.
@@ -357,7 +343,7 @@ __device__ __forceinline__ void epilogue_running(const TcdShared &sh, const TcdT
                      "r"(rl[0]), "r"(rl[1]), "r"(rl[2]), "r"(rl[3]), "r"(rl[4]), "r"(rl[5]), "r"(rl[6]), "r"(rl[7])
                      : "memory");
     }
-    tmem_wait_st();
+    tc::tmem_wait_st();
 }
 
 // E^P of this thread (16 columns, double-float) from / to tensor memory.
@@ -366,9 +352,9 @@ __device__ __forceinline__ void load_ep(uint32_t taddr, float (&hi)[16], float (
     tc::tmem_ld16(taddr + 16, lo);
 }
 __device__ __forceinline__ void store_ep(uint32_t taddr, const float (&hi)[16], const float (&lo)[16]) {
-    tmem_st16(taddr, hi);
-    tmem_st16(taddr + 16, lo);
-    tmem_wait_st();
+    tc::tmem_st16(taddr, hi);
+    tc::tmem_st16(taddr + 16, lo);
+    tc::tmem_wait_st();
 }
 
 // acc += w h for a double-float real w and a float h; the compensation term

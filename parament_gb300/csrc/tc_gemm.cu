@@ -16,15 +16,20 @@
 // and D accumulates hi*hi + hi*lo + lo*hi in FP32 (TMEM), which keeps the
 // products near FP32 accuracy.
 //
-// Warp roles.  Warp 8 (one thread) issues the tiled TMA copies of the A and B
-// slabs into a four-deep raw ring (A lands already in the 128-byte-swizzled
-// K-major operand layout) and the tcgen05.mma instructions of each converted
-// stage, committing them to the stage's "empty" mbarrier.  Warps 0-7 split
-// each raw slab into the hi / lo operand tiles of one of two stages with
-// 16-byte shared-memory accesses and arrive on the stage's "full" mbarrier;
-// at the end of a batch item they read the accumulators with tcgen05.ld into
-// a padded staging tile and write the item's rows with coalesced 16-byte
-// accesses.
+// Warp roles.  Warp 16 (one thread) issues the tiled TMA copies of the A and B
+// slabs into a five-deep raw ring (A lands 128-byte swizzled, so that a warp
+// reading one row per lane meets no bank conflicts) and the tcgen05.mma
+// instructions of each converted stage, committing them to the stage's
+// "empty" mbarrier.  Warps 0-15 split each raw slab into hi / lo operands of
+// one of three stages - A into tensor memory (tcgen05.st, one row per lane), B''
+// into 128-byte-swizzled K-major shared memory with 16-byte stores - and arrive
+// on the stage's "full" mbarrier.  With A in tensor memory the MMAs read only
+// B'' from shared memory.  At the end of a batch item the converter warps read
+// the accumulators with tcgen05.ld into a swizzled staging tile and write the
+// item's rows with coalesced 16-byte accesses.
+//
+// Tensor memory (512 columns allocated): accumulator D in columns 0-127;
+// stage s keeps A' hi in columns 128 + 64 s .. +31 and A' lo in the next 32.
 #include <cuda.h>
 #include <stdlib.h>
 
@@ -36,14 +41,14 @@
 
 namespace pgb {
 
-constexpr int kTcStages = 2;
+constexpr int kTcStages = 3;
 constexpr int kTcTileBytes = 128 * 128;  // 128 rows x 32 FP32 = 16 KB
-constexpr int kTcStageBytes = 4 * kTcTileBytes;
+constexpr int kTcStageBytes = 2 * kTcTileBytes;  // B'' hi and lo (A lives in tensor memory)
 constexpr uint32_t kTcWaitLimit = 1u << 22;
 // Raw complex64 slabs arrive by tiled TMA copies into a ring of kTcRaw
 // stages: A rows r0..r0+127 x 16 complex columns (128 bytes per row), then B
 // rows 16 kc .. 16 kc + 15 x 64 complex columns (512 bytes per row).
-constexpr int kTcRaw = 4;
+constexpr int kTcRaw = 5;
 constexpr int kTcRawA = 128 * 128;
 constexpr int kTcRawB = 16 * 512;
 constexpr int kTcRawStage = kTcRawA + kTcRawB;
@@ -109,35 +114,52 @@ __device__ __forceinline__ void put_split4(uint32_t hi_addr, uint32_t lo_addr, f
 __device__ __forceinline__ void tc_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_addr(bar)) : "memory");
 }
-// Barrier 1 among the 256 converter threads (the issuer warp does not take part).
-__device__ __forceinline__ void conv_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+constexpr int kTcConv = 256;       // converter threads: warps 0-7
+constexpr int kTcIssuer = 8;       // warp 8 issues the copies and the MMAs
+constexpr int kTcEpi = 9;          // warps 9-12 drain the accumulators
+constexpr int kTcThreads = (kTcEpi + 4) * 32;
+constexpr int kTcTmemCols = 512;
+constexpr int kTcAccCols = 128;    // accumulator a in columns 128 a .. +127
+constexpr int kTcAcol = 256;       // stage s: A' hi in columns 256 + 64 s .. +31, lo in the next 32
 
-constexpr int kTcThreads = 288;     // warps 0-7 convert, warp 8 issues copies and MMAs
-constexpr int kTcStagePitch = 528;  // bytes per row of the epilogue's staging tile (64 complex + 16)
+// Work unit k of a CTA: tile (128 rows x 64 complex columns) of batch item b.
+struct TcWork {
+    int b, r0, c0;
+};
+__device__ __forceinline__ TcWork tc_work(const TcArgs &g, int k) {
+    const long long w = (long long)blockIdx.x + (long long)k * gridDim.x;
+    const int ntiles = (g.d / 128) * g.tiles_n;
+    const int tile = (int)(w % ntiles);
+    return TcWork{(int)(w / ntiles), (tile / g.tiles_n) * 128, (tile % g.tiles_n) * 64};
+}
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constant__ TcArgs g) {
     extern __shared__ unsigned char smem_dyn[];
     __shared__ uint64_t empty[kTcStages];  // MMAs that read a converted stage completed
-    __shared__ uint64_t full[kTcStages];   // the 256 converter threads filled a stage
+    __shared__ uint64_t full[kTcStages];   // the converter threads filled a stage
     __shared__ uint64_t rawbar[kTcRaw];    // the TMA copies of a raw stage landed
+    __shared__ uint64_t accf[2];           // every MMA of the unit in accumulator a completed
+    __shared__ uint64_t acce[2];           // the epilogue warps read accumulator a
     __shared__ uint32_t tmem_base;
     unsigned char *smem = smem_dyn + ((1024u - (tc::smem_addr(smem_dyn) & 1023u)) & 1023u);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int d = g.d;
-    const int tile = blockIdx.x;
-    const int r0 = (tile / g.tiles_n) * 128, c0 = (tile % g.tiles_n) * 64;
     const uint32_t idesc = tc::idesc_tf32(128, 128);
 
-    if (warp == 8) {
-        tc::tmem_alloc(&tmem_base, 128);
+    if (warp == kTcIssuer) {
+        tc::tmem_alloc(&tmem_base, kTcTmemCols);
         tc::tmem_relinquish();
     }
     if (tid == 0) {
         for (int s = 0; s < kTcStages; ++s) {
             tc::mbar_init(&empty[s], 1);
-            tc::mbar_init(&full[s], 256);
+            tc::mbar_init(&full[s], kTcConv);
         }
         for (int s = 0; s < kTcRaw; ++s) tc::mbar_init(&rawbar[s], 1);
+        for (int a = 0; a < 2; ++a) {
+            tc::mbar_init(&accf[a], 1);
+            tc::mbar_init(&acce[a], 128);
+        }
         tc::fence_mbar_init();
     }
     tc::fence_before_sync();
@@ -146,163 +168,170 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
     const uint32_t taddr = tmem_base;
     bool ok = true;
 
-    // The CTA's slabs q = j nk + kc run over its batch items b = blockIdx.y +
-    // j gridDim.y and their K slabs kc.  Slab q is converted into stage q % 2;
-    // its raw data sits in raw stage q % kTcRaw.  The n-th completion of a
-    // barrier has phase parity n & 1.
+    // The CTA's work units k = 0, 1, ... (tc_work) each run over the K slabs
+    // kc of their tile: slab q = k nk + kc is converted into stage q % kTcStages
+    // from raw stage q % kTcRaw, and unit k accumulates in accumulator k % 2.
+    // The n-th completion of a barrier has phase parity n & 1.
     const int nk = d / 16;
-    const int nitems = (g.batch - (int)blockIdx.y + (int)gridDim.y - 1) / (int)gridDim.y;
-    const int nslab = nitems * nk;
+    const long long total = (long long)((d / 128) * g.tiles_n) * g.batch;
+    const int nunits = (int)((total - (long long)blockIdx.x + gridDim.x - 1) / gridDim.x);
+    const int nslab = nunits * nk;
     unsigned char *raw0 = smem + (size_t)kTcStages * kTcStageBytes;
 
-    if (warp == 8) {
+    if (warp == kTcIssuer) {
         if (lane == 0) {
-            int jn = 0, kn = 0;  // item and slab of the next raw copy
+            int kn = 0, kcn = 0;  // unit and slab of the next raw copy
+            TcWork wn = tc_work(g, 0);
             auto issue_raw = [&](int q) {
                 const int st = q % kTcRaw;
                 unsigned char *ra = raw0 + st * kTcRawStage, *rb = ra + kTcRawA;
-                const int b = (int)blockIdx.y + jn * (int)gridDim.y;
                 tc_expect_tx(&rawbar[st], kTcRawA + kTcRawB);
-                tc_tma_load3(ra, &g.tmA, 32 * kn, r0, g.batchedA ? b : 0, &rawbar[st]);
-                tc_tma_load3(rb, &g.tmB, 2 * c0, 16 * kn, g.batchedB ? b : 0, &rawbar[st]);
-                if (++kn == nk) kn = 0, ++jn;
+                tc_tma_load3(ra, &g.tmA, 32 * kcn, wn.r0, g.batchedA ? wn.b : 0, &rawbar[st]);
+                tc_tma_load3(rb, &g.tmB, 2 * wn.c0, 16 * kcn, g.batchedB ? wn.b : 0, &rawbar[st]);
+                if (++kcn == nk) kcn = 0, wn = tc_work(g, ++kn);
             };
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&g.tmA)) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&g.tmB)) : "memory");
             for (int q = 0; q < kTcRaw && q < nslab; ++q) issue_raw(q);
-            int kc = 0;
+            int kc = 0, k = 0;
             for (int q = 0; q < nslab; ++q) {
-                const int s = q & 1;
-                if (!tc::mbar_wait(&full[s], (uint32_t)(q >> 1) & 1, kTcWaitLimit)) ok = false;
+                const int s = q % kTcStages, a = k & 1;
+                if (kc == 0 && k >= 2) {
+                    // The epilogue warps read accumulator a for unit k - 2.
+                    if (!tc::mbar_wait(&acce[a], (uint32_t)((k - 2) >> 1) & 1, kTcWaitLimit)) ok = false;
+                }
+                if (!tc::mbar_wait(&full[s], (uint32_t)(q / kTcStages) & 1, kTcWaitLimit)) ok = false;
                 tc::fence_after_sync();
-                const uint32_t ah = tc::smem_addr(smem + s * kTcStageBytes), al = ah + kTcTileBytes;
-                const uint32_t bh = al + kTcTileBytes, bl = bh + kTcTileBytes;
+                const uint32_t acc = taddr + kTcAccCols * a;
+                const uint32_t ah = taddr + kTcAcol + 64 * s, al = ah + 32;
+                const uint32_t bh = tc::smem_addr(smem + s * kTcStageBytes), bl = bh + kTcTileBytes;
 #pragma unroll
                 for (int k8 = 0; k8 < 4; ++k8) {
-                    const uint32_t o = 32 * k8;  // 8 TF32 = 32 bytes along K
-                    tc::mma_tf32(taddr, tc::desc_k_sw128(ah + o), tc::desc_k_sw128(bh + o), idesc,
-                                 (kc > 0 || k8 > 0) ? 1u : 0u);
-                    tc::mma_tf32(taddr, tc::desc_k_sw128(ah + o), tc::desc_k_sw128(bl + o), idesc, 1u);
-                    tc::mma_tf32(taddr, tc::desc_k_sw128(al + o), tc::desc_k_sw128(bh + o), idesc, 1u);
+                    const uint32_t o = 32 * k8;  // 8 TF32 = 32 bytes along a K-major row
+                    tc::mma_tf32_ta(acc, ah + 8 * k8, tc::desc_k_sw128(bh + o), idesc, (kc > 0 || k8 > 0) ? 1u : 0u);
+                    tc::mma_tf32_ta(acc, ah + 8 * k8, tc::desc_k_sw128(bl + o), idesc, 1u);
+                    tc::mma_tf32_ta(acc, al + 8 * k8, tc::desc_k_sw128(bh + o), idesc, 1u);
                 }
                 tc::mma_commit(&empty[s]);
+                if (kc == nk - 1) tc::mma_commit(&accf[a]);
                 // The converters read raw stage q % kTcRaw before they arrived on full[s].
                 if (q + kTcRaw < nslab) issue_raw(q + kTcRaw);
-                if (++kc == nk) kc = 0;
+                if (++kc == nk) kc = 0, ++k;
             }
         }
         __syncwarp();
-    } else {
-        unsigned char *stg = smem;  // epilogue staging tile: 128 rows x kTcStagePitch bytes
-        const uint32_t stg_a = tc::smem_addr(stg);
-        int j = 0, kc = 0;
+    } else if (warp < kTcIssuer) {
+        int k = 0, kc = 0;
+        TcWork wk = tc_work(g, 0);
         for (int q = 0; q < nslab; ++q) {
-            const int s = q & 1, rs = q % kTcRaw;
-            // The MMAs of slab q - 2 read stage s.
-            if (q >= 2 && !tc::mbar_wait(&empty[s], (uint32_t)((q - 2) >> 1) & 1, kTcWaitLimit)) ok = false;
+            const int s = q % kTcStages, rs = q % kTcRaw;
+            // The MMAs of slab q - kTcStages read stage s.
+            if (q >= kTcStages &&
+                !tc::mbar_wait(&empty[s], (uint32_t)((q - kTcStages) / kTcStages) & 1, kTcWaitLimit))
+                ok = false;
             if (!tc::mbar_wait(&rawbar[rs], (uint32_t)(q / kTcRaw) & 1, kTcWaitLimit)) ok = false;
+            tc::fence_after_sync();
             const uint32_t ra = tc::smem_addr(raw0 + rs * kTcRawStage), rb = ra + kTcRawA;
-            const uint32_t ah = tc::smem_addr(smem + s * kTcStageBytes), al = ah + kTcTileBytes;
-            const uint32_t bh = al + kTcTileBytes, bl = bh + kTcTileBytes;
-            // A' slab (rows r0..r0+127, complex columns 16 kc .. 16 kc + 15): the
-            // TMA copy left it in the operand layout, so hi and lo go to the same
-            // offsets.  Chunk f holds complex columns 2 ch, 2 ch + 1 of row f / 8.
+            const uint32_t bh = tc::smem_addr(smem + s * kTcStageBytes), bl = bh + kTcTileBytes;
+            // A' slab (rows r0..r0+127, complex columns 16 kc .. 16 kc + 15) into
+            // tensor memory: warp w writes lanes 32 (w % 4) .. +31, K values
+            // 16 (w / 4) .. +15 of one row per lane.  Logical 16-byte chunk c of
+            // the row (complex columns 2c, 2c + 1) sits at chunk c ^ (row % 8).
+            {
+                const int wq = warp & 3, h = warp >> 2, rl = 32 * wq + lane;
+                float hi[16], lo[16];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int f = tid + 256 * i;
-                float4 x = lds128(ra + 16 * f);
-                if (g.a_minus_identity) {
-                    const int row = f >> 3, ch = (f & 7) ^ (row & 7);
-                    const int dk = r0 + row - 16 * kc - 2 * ch;
-                    if (dk == 0) x.x -= 1.0f;
-                    if (dk == 1) x.z -= 1.0f;
+                for (int i = 0; i < 4; ++i) {
+                    const int c = 4 * h + i;
+                    float4 x = lds128(ra + rl * 128 + 16 * (c ^ (rl & 7)));
+                    if (g.a_minus_identity) {
+                        const int dk = wk.r0 + rl - 16 * kc - 2 * c;
+                        if (dk == 0) x.x -= 1.0f;
+                        if (dk == 1) x.z -= 1.0f;
+                    }
+                    const float v[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        hi[4 * i + e] = tf32_rna(v[e]);
+                        lo[4 * i + e] = tf32_rna(v[e] - hi[4 * i + e]);
+                    }
                 }
-                put_split4(ah + 16 * f, al + 16 * f, x);
+                const uint32_t ta = taddr + ((uint32_t)(32 * wq) << 16) + kTcAcol + 64 * s + 16 * h;
+                tc::tmem_st16(ta, hi);
+                tc::tmem_st16(ta + 32, lo);
             }
             // B''^T slab (rows n, 32 K values): task (n, c) writes K = 4c .. 4c + 3
             // of rows n and 64 + n from B rows 2c, 2c + 1 (raw rows of 512 bytes).
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
-                const int t = tid + 256 * i, n = t & 63, c = t >> 6;
+                const int t = tid + kTcConv * i, n = t & 63, c = t >> 6;
                 const float2 v0 = lds64(rb + (uint32_t)((2 * c) * 64 + n) * 8);
                 const float2 v1 = lds64(rb + (uint32_t)((2 * c + 1) * 64 + n) * 8);
                 const uint32_t o_re = tc::sw128_offset(n, 4 * c), o_im = tc::sw128_offset(64 + n, 4 * c);
                 put_split4(bh + o_re, bl + o_re, make_float4(v0.x, -v0.y, v1.x, -v1.y));
                 put_split4(bh + o_im, bl + o_im, make_float4(v0.y, v0.x, v1.y, v1.x));
             }
+            tc::tmem_wait_st();
             tc::fence_proxy_async();
-            tc_arrive(&full[s]);
-            if (++kc < nk) continue;
-            kc = 0;
-            // Last slab of item b: its commit covers every MMA of the item.
-            const int b = (int)blockIdx.y + j * (int)gridDim.y;
-            ++j;
-            if (!tc::mbar_wait(&empty[s], (uint32_t)(q >> 1) & 1, kTcWaitLimit)) ok = false;
-            tc::fence_after_sync();
-            // Epilogue, first half: warp w reads TMEM lanes 32 (w % 4) .. +31
-            // (rows of the tile), complex columns 32 (w / 4) .. +31, into the
-            // staging tile (both stages are idle until the next item).
-            {
-                const int wq = warp & 3, half = warp >> 2, rl = 32 * wq + lane;
-                const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
-#pragma unroll
-                for (int cc = 0; cc < 2; ++cc) {
-                    const int col0 = 32 * half + 16 * cc;
-                    float re[16], im[16];
-                    tc::tmem_ld16(taddr + lane_base + col0, re);
-                    tc::tmem_ld16(taddr + lane_base + 64 + col0, im);
-#pragma unroll
-                    for (int jj = 0; jj < 8; ++jj)
-                        sts128(stg_a + rl * kTcStagePitch + (col0 + 2 * jj) * 8,
-                               make_float4(re[2 * jj], im[2 * jj], re[2 * jj + 1], im[2 * jj + 1]));
-                }
-            }
             tc::fence_before_sync();
-            conv_sync();
-            // Second half: rows of the tile, 16 bytes (two complex) per thread;
-            // the sixteen Cin loads are all in flight before the first use.
-            {
-                const float2 *Cin = g.Cin ? g.Cin + (size_t)b * g.sCin : nullptr;
-                float2 *Co = g.Cout + (size_t)b * g.sCout;
-                float4 ci[16];
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int idx = tid + 256 * i, rl = idx >> 5, c4 = idx & 31;
-                    ci[i] = Cin ? *reinterpret_cast<const float4 *>(Cin + (size_t)(r0 + rl) * d + c0 + 2 * c4)
-                                : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int idx = tid + 256 * i, rl = idx >> 5, c4 = idx & 31;
-                    const float4 v = lds128(stg_a + rl * kTcStagePitch + 16 * c4);
-                    const int row = r0 + rl, col = c0 + 2 * c4;
-                    const size_t e = (size_t)row * d + col;
-                    float4 o = make_float4(g.alpha.x * v.x - g.alpha.y * v.y, g.alpha.x * v.y + g.alpha.y * v.x,
-                                           g.alpha.x * v.z - g.alpha.y * v.w, g.alpha.x * v.w + g.alpha.y * v.z);
-                    if (Cin) {
-                        o.x += g.beta * ci[i].x;
-                        o.y += g.beta * ci[i].y;
-                        o.z += g.beta * ci[i].z;
-                        o.w += g.beta * ci[i].w;
-                    }
-                    if (row == col) o.x += g.diag.x, o.y += g.diag.y;
-                    if (row == col + 1) o.z += g.diag.x, o.w += g.diag.y;
-                    if (ok) *reinterpret_cast<float4 *>(Co + e) = o;
-                }
-            }
-            // The staging tile is read before the next item's slabs overwrite it.
-            conv_sync();
+            tc_arrive(&full[s]);
+            if (++kc == nk) kc = 0, wk = tc_work(g, ++k);
         }
         // Every raw copy was waited for in the loop; a wait that gave up is
         // tried once more so that no copy lands after the CTA has exited.
         if (!ok)
             for (int q = (nslab > kTcRaw ? nslab - kTcRaw : 0); q < nslab; ++q)
                 tc::mbar_wait(&rawbar[q % kTcRaw], (uint32_t)(q / kTcRaw) & 1, kTcWaitLimit);
+    } else {
+        // Epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. +31, one row of
+        // the tile per lane, 16 complex columns at a time, and writes
+        //   C = alpha D + beta Cin + diag I
+        // for its row with 16-byte accesses.
+        const int wq = warp & 3, rl = 32 * wq + lane;
+        for (int k = 0; k < nunits; ++k) {
+            const TcWork wk = tc_work(g, k);
+            const int a = k & 1;
+            if (!tc::mbar_wait(&accf[a], (uint32_t)(k >> 1) & 1, kTcWaitLimit)) ok = false;
+            tc::fence_after_sync();
+            const int row = wk.r0 + rl;
+            const float2 *Cin = g.Cin ? g.Cin + (size_t)wk.b * g.sCin + (size_t)row * d + wk.c0 : nullptr;
+            float2 *Co = g.Cout + (size_t)wk.b * g.sCout + (size_t)row * d + wk.c0;
+            const uint32_t acc = taddr + ((uint32_t)(32 * wq) << 16) + kTcAccCols * a;
+#pragma unroll 1
+            for (int cc = 0; cc < 4; ++cc) {
+                float4 ci[8];
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj)
+                    ci[jj] = Cin ? *reinterpret_cast<const float4 *>(Cin + 16 * cc + 2 * jj)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+                float re[16], im[16];
+                tc::tmem_ld16(acc + 16 * cc, re);
+                tc::tmem_ld16(acc + 64 + 16 * cc, im);
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) {
+                    const int col = wk.c0 + 16 * cc + 2 * jj;
+                    const float xr = re[2 * jj], xi = im[2 * jj], yr = re[2 * jj + 1], yi = im[2 * jj + 1];
+                    float4 o = make_float4(g.alpha.x * xr - g.alpha.y * xi, g.alpha.x * xi + g.alpha.y * xr,
+                                           g.alpha.x * yr - g.alpha.y * yi, g.alpha.x * yi + g.alpha.y * yr);
+                    o.x += g.beta * ci[jj].x;
+                    o.y += g.beta * ci[jj].y;
+                    o.z += g.beta * ci[jj].z;
+                    o.w += g.beta * ci[jj].w;
+                    if (row == col) o.x += g.diag.x, o.y += g.diag.y;
+                    if (row == col + 1) o.z += g.diag.x, o.w += g.diag.y;
+                    if (ok) *reinterpret_cast<float4 *>(Co + 16 * cc + 2 * jj) = o;
+                }
+            }
+            tc::fence_before_sync();
+            tc_arrive(&acce[a]);
+        }
     }
     if (!ok) atomicAdd(&g_tc_faults, 1);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 8) {
+    if (warp == kTcIssuer) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(taddr, 128);
+        tc::tmem_dealloc(taddr, kTcTmemCols);
     }
 }
 
@@ -380,7 +409,10 @@ cudaError_t launch_tc_gemm(const GemmLaunch &l) {
     cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_tc_cgemm),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((l.d / 128) * (l.d / 64), std::min(l.batch, 65535));
+    // Persistent grid: one CTA per SM walks the (tile, item) units.
+    const long long units = (long long)(l.d / 128) * (l.d / 64) * l.batch;
+    const int sms = l.num_sms > 0 ? l.num_sms : 148;
+    const int grid = (int)std::min<long long>(units, sms);
     k_tc_cgemm<<<grid, kTcThreads, smem, l.stream>>>(g);
     return cudaGetLastError();
 }
