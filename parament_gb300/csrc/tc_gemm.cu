@@ -41,16 +41,16 @@
 
 namespace pgb {
 
-constexpr int kTcStages = 3;
-constexpr int kTcTileBytes = 128 * 128;  // 128 rows x 32 FP32 = 16 KB
+constexpr int kTcStages = 2;
+constexpr int kTcTileBytes = 256 * 128;  // B'' slab: 256 rows x 32 FP32 = 32 KB
 constexpr int kTcStageBytes = 2 * kTcTileBytes;  // B'' hi and lo (A lives in tensor memory)
 constexpr uint32_t kTcWaitLimit = 1u << 22;
 // Raw complex64 slabs arrive by tiled TMA copies into a ring of kTcRaw
 // stages: A rows r0..r0+127 x 16 complex columns (128 bytes per row), then B
-// rows 16 kc .. 16 kc + 15 x 64 complex columns (512 bytes per row).
-constexpr int kTcRaw = 5;
+// rows 16 kc .. 16 kc + 15 x 128 complex columns (1024 bytes per row).
+constexpr int kTcRaw = 3;
 constexpr int kTcRawA = 128 * 128;
-constexpr int kTcRawB = 16 * 512;
+constexpr int kTcRawB = 16 * 1024;
 constexpr int kTcRawStage = kTcRawA + kTcRawB;
 constexpr size_t kTcSmem = (size_t)kTcStages * kTcStageBytes + (size_t)kTcRaw * kTcRawStage + 1024;
 static_assert(kTcSmem <= 232448, "shared memory of k_tc_cgemm exceeds 227 KB");
@@ -116,13 +116,13 @@ __device__ __forceinline__ void tc_arrive(uint64_t *bar) {
 }
 constexpr int kTcConv = 256;       // converter threads: warps 0-7
 constexpr int kTcIssuer = 8;       // warp 8 issues the copies and the MMAs
-constexpr int kTcEpi = 9;          // warps 9-12 drain the accumulators
-constexpr int kTcThreads = (kTcEpi + 4) * 32;
-constexpr int kTcTmemCols = 512;
-constexpr int kTcAccCols = 128;    // accumulator a in columns 128 a .. +127
+constexpr int kTcEpi = 9;          // warps 9-16 drain the accumulator
+constexpr int kTcEpiThreads = 256;
+constexpr int kTcThreads = kTcEpi * 32 + kTcEpiThreads;
+constexpr int kTcTmemCols = 512;   // accumulator D in columns 0-255
 constexpr int kTcAcol = 256;       // stage s: A' hi in columns 256 + 64 s .. +31, lo in the next 32
 
-// Work unit k of a CTA: tile (128 rows x 64 complex columns) of batch item b.
+// Work unit k of a CTA: tile (128 rows x 128 complex columns) of batch item b.
 struct TcWork {
     int b, r0, c0;
 };
@@ -130,7 +130,7 @@ __device__ __forceinline__ TcWork tc_work(const TcArgs &g, int k) {
     const long long w = (long long)blockIdx.x + (long long)k * gridDim.x;
     const int ntiles = (g.d / 128) * g.tiles_n;
     const int tile = (int)(w % ntiles);
-    return TcWork{(int)(w / ntiles), (tile / g.tiles_n) * 128, (tile % g.tiles_n) * 64};
+    return TcWork{(int)(w / ntiles), (tile / g.tiles_n) * 128, (tile % g.tiles_n) * 128};
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constant__ TcArgs g) {
@@ -138,13 +138,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
     __shared__ uint64_t empty[kTcStages];  // MMAs that read a converted stage completed
     __shared__ uint64_t full[kTcStages];   // the converter threads filled a stage
     __shared__ uint64_t rawbar[kTcRaw];    // the TMA copies of a raw stage landed
-    __shared__ uint64_t accf[2];           // every MMA of the unit in accumulator a completed
-    __shared__ uint64_t acce[2];           // the epilogue warps read accumulator a
+    __shared__ uint64_t accf;              // every MMA of the unit completed
+    __shared__ uint64_t acce;              // the epilogue warps read the accumulator
     __shared__ uint32_t tmem_base;
     unsigned char *smem = smem_dyn + ((1024u - (tc::smem_addr(smem_dyn) & 1023u)) & 1023u);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int d = g.d;
-    const uint32_t idesc = tc::idesc_tf32(128, 128);
+    const uint32_t idesc = tc::idesc_tf32(128, 256);
 
     if (warp == kTcIssuer) {
         tc::tmem_alloc(&tmem_base, kTcTmemCols);
@@ -156,10 +156,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
             tc::mbar_init(&full[s], kTcConv);
         }
         for (int s = 0; s < kTcRaw; ++s) tc::mbar_init(&rawbar[s], 1);
-        for (int a = 0; a < 2; ++a) {
-            tc::mbar_init(&accf[a], 1);
-            tc::mbar_init(&acce[a], 128);
-        }
+        tc::mbar_init(&accf, 1);
+        tc::mbar_init(&acce, kTcEpiThreads);
         tc::fence_mbar_init();
     }
     tc::fence_before_sync();
@@ -170,8 +168,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
 
     // The CTA's work units k = 0, 1, ... (tc_work) each run over the K slabs
     // kc of their tile: slab q = k nk + kc is converted into stage q % kTcStages
-    // from raw stage q % kTcRaw, and unit k accumulates in accumulator k % 2.
-    // The n-th completion of a barrier has phase parity n & 1.
+    // from raw stage q % kTcRaw.  The n-th completion of a barrier has phase
+    // parity n & 1.
     const int nk = d / 16;
     const long long total = (long long)((d / 128) * g.tiles_n) * g.batch;
     const int nunits = (int)((total - (long long)blockIdx.x + gridDim.x - 1) / gridDim.x);
@@ -195,14 +193,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
             for (int q = 0; q < kTcRaw && q < nslab; ++q) issue_raw(q);
             int kc = 0, k = 0;
             for (int q = 0; q < nslab; ++q) {
-                const int s = q % kTcStages, a = k & 1;
-                if (kc == 0 && k >= 2) {
-                    // The epilogue warps read accumulator a for unit k - 2.
-                    if (!tc::mbar_wait(&acce[a], (uint32_t)((k - 2) >> 1) & 1, kTcWaitLimit)) ok = false;
+                const int s = q % kTcStages;
+                if (kc == 0 && k >= 1) {
+                    // The epilogue warps read the accumulator of unit k - 1.
+                    if (!tc::mbar_wait(&acce, (uint32_t)(k - 1) & 1, kTcWaitLimit)) ok = false;
                 }
                 if (!tc::mbar_wait(&full[s], (uint32_t)(q / kTcStages) & 1, kTcWaitLimit)) ok = false;
                 tc::fence_after_sync();
-                const uint32_t acc = taddr + kTcAccCols * a;
+                const uint32_t acc = taddr;
                 const uint32_t ah = taddr + kTcAcol + 64 * s, al = ah + 32;
                 const uint32_t bh = tc::smem_addr(smem + s * kTcStageBytes), bl = bh + kTcTileBytes;
 #pragma unroll
@@ -213,7 +211,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
                     tc::mma_tf32_ta(acc, al + 8 * k8, tc::desc_k_sw128(bh + o), idesc, 1u);
                 }
                 tc::mma_commit(&empty[s]);
-                if (kc == nk - 1) tc::mma_commit(&accf[a]);
+                if (kc == nk - 1) tc::mma_commit(&accf);
                 // The converters read raw stage q % kTcRaw before they arrived on full[s].
                 if (q + kTcRaw < nslab) issue_raw(q + kTcRaw);
                 if (++kc == nk) kc = 0, ++k;
@@ -261,13 +259,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
                 tc::tmem_st16(ta + 32, lo);
             }
             // B''^T slab (rows n, 32 K values): task (n, c) writes K = 4c .. 4c + 3
-            // of rows n and 64 + n from B rows 2c, 2c + 1 (raw rows of 512 bytes).
+            // of rows n and 128 + n from B rows 2c, 2c + 1 (raw rows of 1024 bytes).
 #pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                const int t = tid + kTcConv * i, n = t & 63, c = t >> 6;
-                const float2 v0 = lds64(rb + (uint32_t)((2 * c) * 64 + n) * 8);
-                const float2 v1 = lds64(rb + (uint32_t)((2 * c + 1) * 64 + n) * 8);
-                const uint32_t o_re = tc::sw128_offset(n, 4 * c), o_im = tc::sw128_offset(64 + n, 4 * c);
+            for (int i = 0; i < 4; ++i) {
+                const int t = tid + kTcConv * i, n = t & 127, c = t >> 7;
+                const float2 v0 = lds64(rb + (uint32_t)((2 * c) * 128 + n) * 8);
+                const float2 v1 = lds64(rb + (uint32_t)((2 * c + 1) * 128 + n) * 8);
+                const uint32_t o_re = tc::sw128_offset(n, 4 * c), o_im = tc::sw128_offset(128 + n, 4 * c);
                 put_split4(bh + o_re, bl + o_re, make_float4(v0.x, -v0.y, v1.x, -v1.y));
                 put_split4(bh + o_im, bl + o_im, make_float4(v0.y, v0.x, v1.y, v1.x));
             }
@@ -284,19 +282,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
                 tc::mbar_wait(&rawbar[q % kTcRaw], (uint32_t)(q / kTcRaw) & 1, kTcWaitLimit);
     } else {
         // Epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. +31, one row of
-        // the tile per lane, 16 complex columns at a time, and writes
-        //   C = alpha D + beta Cin + diag I
-        // for its row with 16-byte accesses.
-        const int wq = warp & 3, rl = 32 * wq + lane;
+        // the tile per lane, complex columns 64 h .. 64 h + 63 (h = (w - 9) / 4)
+        // 16 at a time, and writes  C = alpha D + beta Cin + diag I  for its row
+        // with 16-byte accesses.  The accumulator is released after the last
+        // tensor-memory load, before the last stores.
+        const int wq = warp & 3, h = (warp - kTcEpi) >> 2, rl = 32 * wq + lane;
         for (int k = 0; k < nunits; ++k) {
             const TcWork wk = tc_work(g, k);
-            const int a = k & 1;
-            if (!tc::mbar_wait(&accf[a], (uint32_t)(k >> 1) & 1, kTcWaitLimit)) ok = false;
+            if (!tc::mbar_wait(&accf, (uint32_t)k & 1, kTcWaitLimit)) ok = false;
             tc::fence_after_sync();
-            const int row = wk.r0 + rl;
-            const float2 *Cin = g.Cin ? g.Cin + (size_t)wk.b * g.sCin + (size_t)row * d + wk.c0 : nullptr;
-            float2 *Co = g.Cout + (size_t)wk.b * g.sCout + (size_t)row * d + wk.c0;
-            const uint32_t acc = taddr + ((uint32_t)(32 * wq) << 16) + kTcAccCols * a;
+            const int row = wk.r0 + rl, cb = wk.c0 + 64 * h;
+            const float2 *Cin = g.Cin ? g.Cin + (size_t)wk.b * g.sCin + (size_t)row * d + cb : nullptr;
+            float2 *Co = g.Cout + (size_t)wk.b * g.sCout + (size_t)row * d + cb;
+            const uint32_t acc = taddr + ((uint32_t)(32 * wq) << 16) + 64 * h;
 #pragma unroll 1
             for (int cc = 0; cc < 4; ++cc) {
                 float4 ci[8];
@@ -306,10 +304,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
                                  : make_float4(0.f, 0.f, 0.f, 0.f);
                 float re[16], im[16];
                 tc::tmem_ld16(acc + 16 * cc, re);
-                tc::tmem_ld16(acc + 64 + 16 * cc, im);
+                tc::tmem_ld16(acc + 128 + 16 * cc, im);
+                if (cc == 3) {
+                    tc::fence_before_sync();
+                    tc_arrive(&acce);
+                }
 #pragma unroll
                 for (int jj = 0; jj < 8; ++jj) {
-                    const int col = wk.c0 + 16 * cc + 2 * jj;
+                    const int col = cb + 16 * cc + 2 * jj;
                     const float xr = re[2 * jj], xi = im[2 * jj], yr = re[2 * jj + 1], yi = im[2 * jj + 1];
                     float4 o = make_float4(g.alpha.x * xr - g.alpha.y * xi, g.alpha.x * xi + g.alpha.y * xr,
                                            g.alpha.x * yr - g.alpha.y * yi, g.alpha.x * yi + g.alpha.y * yr);
@@ -322,8 +324,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
                     if (ok) *reinterpret_cast<float4 *>(Co + 16 * cc + 2 * jj) = o;
                 }
             }
-            tc::fence_before_sync();
-            tc_arrive(&acce[a]);
         }
     }
     if (!ok) atomicAdd(&g_tc_faults, 1);
@@ -400,17 +400,17 @@ cudaError_t launch_tc_gemm(const GemmLaunch &l) {
     g.beta = (float)l.beta;
     g.d = l.d;
     g.batch = l.batch;
-    g.tiles_n = l.d / 64;
+    g.tiles_n = l.d / 128;
     g.a_minus_identity = l.a_minus_identity ? 1 : 0;
     if (!make_map(&g.tmA, l.A, l.d, l.strideA, l.batch, 32, 128, CU_TENSOR_MAP_SWIZZLE_128B, &g.batchedA) ||
-        !make_map(&g.tmB, l.B, l.d, l.strideB, l.batch, 128, 16, CU_TENSOR_MAP_SWIZZLE_NONE, &g.batchedB))
+        !make_map(&g.tmB, l.B, l.d, l.strideB, l.batch, 256, 16, CU_TENSOR_MAP_SWIZZLE_NONE, &g.batchedB))
         return cudaErrorInvalidValue;
     const size_t smem = kTcSmem;
     cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_tc_cgemm),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     // Persistent grid: one CTA per SM walks the (tile, item) units.
-    const long long units = (long long)(l.d / 128) * (l.d / 64) * l.batch;
+    const long long units = (long long)(l.d / 128) * (l.d / 128) * l.batch;
     const int sms = l.num_sms > 0 ? l.num_sms : 148;
     const int grid = (int)std::min<long long>(units, sms);
     k_tc_cgemm<<<grid, kTcThreads, smem, l.stream>>>(g);
