@@ -6,30 +6,34 @@
 // SIMT k_gemm: the reference's cublasCgemmStridedBatched calls of the Clenshaw
 // recurrence and the tree (src/cuda/parament.cpp:596-636, :681-690).
 //
-// Real formulation per CTA tile (128 rows x 64 complex columns), per K slab of
-// 16 complex columns of A / rows of B, with K ordered as (re, im) pairs:
-//   D[128 x 128] += A' [128 x 32] * B'' [32 x 128]
+// Real formulation per unit (a tile of 128 rows x 128 complex columns of one
+// batch item), per K slab of 16 complex columns of A / rows of B, with K
+// ordered as (re, im) pairs:
+//   D[128 x 256] += A' [128 x 32] * B'' [32 x 256]
 //   A'[m][2k + p] = (A_r, A_i)[p][m][k]     (the row-major complex data as is)
-//   B''[2k][n]    = B_r[k][n],  B''[2k + 1][n]      = -B_i[k][n]    (n < 64)
-//   B''[2k][64+n] = B_i[k][n],  B''[2k + 1][64 + n] =  B_r[k][n]
+//   B''[2k][n]     = B_r[k][n],  B''[2k + 1][n]       = -B_i[k][n]    (n < 128)
+//   B''[2k][128+n] = B_i[k][n],  B''[2k + 1][128 + n] =  B_r[k][n]
 // so D = [C_r | C_i].  Each FP32 operand is split x = hi + lo with hi, lo TF32
 // and D accumulates hi*hi + hi*lo + lo*hi in FP32 (TMEM), which keeps the
 // products near FP32 accuracy.
 //
-// Warp roles.  Warp 16 (one thread) issues the tiled TMA copies of the A and B
-// slabs into a five-deep raw ring (A lands 128-byte swizzled, so that a warp
-// reading one row per lane meets no bank conflicts) and the tcgen05.mma
-// instructions of each converted stage, committing them to the stage's
-// "empty" mbarrier.  Warps 0-15 split each raw slab into hi / lo operands of
-// one of three stages - A into tensor memory (tcgen05.st, one row per lane), B''
-// into 128-byte-swizzled K-major shared memory with 16-byte stores - and arrive
-// on the stage's "full" mbarrier.  With A in tensor memory the MMAs read only
-// B'' from shared memory.  At the end of a batch item the converter warps read
-// the accumulators with tcgen05.ld into a swizzled staging tile and write the
-// item's rows with coalesced 16-byte accesses.
+// The grid is persistent: one CTA per SM walks the units.  Warp roles:
+//  - warp 8 (one thread) issues the tiled TMA copies of the raw A and B slabs
+//    into a three-deep ring (A lands 128-byte swizzled, so that a warp reading
+//    one row per lane meets no bank conflicts) and, per converted stage, 12
+//    tcgen05.mma (M = 128, N = 256, K = 8, A from tensor memory), committed to
+//    the stage's "empty" mbarrier and, at the end of a unit, to "accf";
+//  - warps 0-7 split each raw slab into the hi / lo operands of one of two
+//    stages - A' into tensor memory (tcgen05.st, one row per lane), B'' into
+//    128-byte-swizzled K-major shared memory with 16-byte stores - and arrive
+//    on the stage's "full" mbarrier;
+//  - warps 9-16 wait for "accf", read the accumulator with tcgen05.ld (one row
+//    per lane, 64 complex columns per warp), arrive on "acce" after the last
+//    load (the issuer waits for it before the next unit's first MMA) and write
+//    C with 16-byte accesses.
 //
-// Tensor memory (512 columns allocated): accumulator D in columns 0-127;
-// stage s keeps A' hi in columns 128 + 64 s .. +31 and A' lo in the next 32.
+// Tensor memory (512 columns): accumulator D in columns 0-255; stage s keeps
+// A' hi in columns 256 + 64 s .. +31 and A' lo in the next 32.
 #include <cuda.h>
 #include <stdlib.h>
 
