@@ -54,7 +54,7 @@ struct Ctx {
     int launches = 0;
 
     // Work buffers (grow-only, like src/cuda/parament.cpp:418-474)
-    DevBuf carr, out, chunks, work, X, B1, B2, aux, grad, wts;
+    DevBuf carr, out, chunks, work, X, B1, B2, aux, grad, wts, xplanes;
 
     size_t esize() const { return fp64 ? 16 : 8; }
     void release_all() {
@@ -70,6 +70,7 @@ struct Ctx {
         aux.release();
         grad.release();
         wts.release();
+        xplanes.release();
     }
 };
 

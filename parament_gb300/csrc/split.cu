@@ -443,11 +443,16 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
     const size_t smem = split_smem(d, (int)c->Ke);
     cudaError_t e = cudaSuccess;
     a.wts = nullptr;
+    a.xplanes = nullptr;
     if (tensor) {
-        // One CTA per SM (tensor-core kernel); the step weights go to a buffer
-        // of P x Ke double-float values first.
-        a.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)c->num_sms, P));
-        if (c->wts.ensure(std::max<size_t>(16, sizeof(float4) * (size_t)P * c->Ke)) != cudaSuccess)
+        // One CTA per SM (tensor-core kernel) per batch of steps; the step
+        // weights go to a buffer of P x Ke double-float values first and the X
+        // planes of a batch to a buffer of kSplitXBatch steps.
+        const long long batches = (P + kSplitXBatch - 1) / kSplitXBatch;
+        a.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)c->num_sms * batches, P));
+        if (c->wts.ensure(std::max<size_t>(16, sizeof(float4) * (size_t)P * c->Ke)) != cudaSuccess ||
+            c->xplanes.ensure(sizeof(float) * kSplitXStride * (size_t)std::min<long long>(P, kSplitXBatch)) !=
+                cudaSuccess)
             return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
         a.wts = static_cast<const float4 *>(c->wts.ptr);
     } else {
@@ -465,16 +470,17 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
         c->aux.ensure(sizeof(double2) * dd) != cudaSuccess)
         return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
     a.chunks = static_cast<double2 *>(c->chunks.ptr);
-    if (c->timing) cudaEventRecord(c->ev_start, stream);
     if (tensor) {
         int nch = 0;
-        e = launch_split_tc(a, c->num_sms, &nch, stream);
+        e = launch_split_tc(a, c->num_sms, static_cast<float *>(c->xplanes.ptr), &nch, stream,
+                            c->timing ? c->ev_start : nullptr, c->timing ? c->ev_stop : nullptr);
         a.nchunks = nch;
     } else {
         void *args[] = {&a};
+        if (c->timing) cudaEventRecord(c->ev_start, stream);
         e = cudaLaunchKernel(fn, dim3(a.nchunks), dim3(256), args, smem, stream);
+        if (c->timing) cudaEventRecord(c->ev_stop, stream);
     }
-    if (c->timing) cudaEventRecord(c->ev_stop, stream);
     int levels = 0;
     if (e == cudaSuccess)
         e = tree_product(true, d, c->chunks.ptr, a.nchunks, c->work.ptr, c->aux.ptr, stream, c->num_sms, &levels);
@@ -483,7 +489,10 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
                                                                    static_cast<float2 *>(d_out), (int)dd);
         e = cudaGetLastError();
     }
-    c->launches = 2 + levels;
+    // Step kernels (tensor form: step weights, then X planes and step kernel
+    // per batch), the tree levels and the final conversion.
+    const long long batches = (P + kSplitXBatch - 1) / kSplitXBatch;
+    c->launches = (tensor ? (c->Ke > 0 ? 1 : 0) + 2 * (int)batches : 1) + levels + 1;
     if (e != cudaSuccess) {
         cudaGetLastError();
         return PARAMENT_STATUS_CUBLAS_FAILED;

@@ -10,6 +10,11 @@ namespace pgb {
 
 constexpr int kSplitMaxOrder = 15;
 constexpr double kSplitMaxX = 0.5;
+// X planes of the tensor-core form: four planes of 64 rows x 68 floats per
+// step (69,632 bytes), formed for batches of up to kSplitXBatch steps at a
+// time (4.6 GB for a full batch).
+constexpr int kSplitXStride = 4 * 64 * 68;
+constexpr long long kSplitXBatch = 65536;
 
 // ---------------------------------------------------------------- double-float
 
@@ -88,6 +93,7 @@ struct SplitArgs {
     int K, amps, mode, magnus;
     double hfac;
     const float4 *wts;                  // P x Ke step weights in double-float (re hi, re lo, im hi, im lo)
+    const float *xplanes;               // X planes of the steps of one launch (tensor-core form)
 };
 
 // Weight m of step s in FP64 from complex64 samples (src/cuda/control_expansion.cu:27-170,
@@ -125,7 +131,13 @@ __device__ __forceinline__ double2 split_weight(const SplitArgs &a, int m, long 
     return cmul(t, f);
 }
 
-// Tensor-core form of the split kernel (split_tc.cu): one CTA per SM.
-cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, int *nchunks, cudaStream_t stream);
+// Tensor-core form of the split kernel (split_tc.cu): for each batch of up
+// to kSplitXBatch steps, the X planes (xplanes: kSplitXBatch x kSplitXStride
+// floats) and then one CTA per SM over the batch.  *nchunks receives the
+// number of chunk products written, at most ceil(P / kSplitXBatch) x num_sms.
+// Non-null ev0 / ev1 are recorded just before the first and after the last
+// step-kernel launch (one batch: around k_split_tc alone).
+cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, float *xplanes, int *nchunks, cudaStream_t stream,
+                            cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 
 }  // namespace pgb

@@ -64,17 +64,16 @@ constexpr uint32_t kTcdWait = 1u << 24;
 constexpr size_t kTcdSA = (size_t)kTcdHi * oz::kASlice;
 constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
 constexpr size_t kTcdSmem = kTcdSA + kTcdSB + 1024;
-// During the assembly the slice buffers are free: they take up to five
-// expansion matrices (32 KB each) at a time, streamed in by bulk copies.
-constexpr int kTcdStageMats = 5;
-constexpr uint32_t kTcdMatBytes = 64 * 64 * 8;
-static_assert(kTcdStageMats * kTcdMatBytes <= kTcdSA + kTcdSB, "staging exceeds the slice buffers");
-// After the assembly X_j passes to the lane layout through four planes of
-// 64 rows padded to 68 floats (conflict-free 16-byte reads of a column block
-// by 32 consecutive rows), also over the slice buffers.
+// X_j reaches the lane layout through four planes (re hi, re lo, im hi, im
+// lo) of 64 rows padded to 68 floats (conflict-free 16-byte reads of a column
+// block by 32 consecutive rows).  k_split_assemble writes them for every step
+// in that layout; one bulk copy per step brings them into the A slice buffer,
+// which is free from the end of a step's last product to the X^2 slicing.
 constexpr int kTcdPlaneLd = 68;
 constexpr int kTcdPlane = 64 * kTcdPlaneLd;
-static_assert(4 * kTcdPlane * sizeof(float) <= kTcdSA + kTcdSB, "planes exceed the slice buffers");
+constexpr uint32_t kTcdXBytes = 4 * kTcdPlane * sizeof(float);
+static_assert(kTcdXBytes <= kTcdSA && kTcdXBytes % 16 == 0, "planes exceed the A slice buffer");
+static_assert(kTcdPlane * 4 == kSplitXStride, "plane layout of k_split_assemble");
 
 __device__ int g_split_tc_faults;
 
@@ -126,11 +125,10 @@ __device__ __forceinline__ void peel8_df(const float (&hi)[8], const float (&lo)
 }
 
 struct TcdShared {
-    float4 ws[2][kTcdMaxKe];       // step weights (double-float re, im), double-buffered across steps
     int amax[2][64], bmax[2][64];
     float rowmul[64], colmul[64];  // 2^(e - 7) of the last A rows / B columns
     uint64_t bar;                  // tensor-core products
-    uint64_t tbar;                 // bulk copies of the expansion matrices
+    uint64_t tbar;                 // bulk copies of the X planes
     uint32_t tmem_base;
 };
 
@@ -452,124 +450,23 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     uint32_t ncommit = 0;
     int nb = 0;  // max-buffer parity
     bool ok = true;
-    // Expansion matrices H_0 .. H_Ke reach shared memory in rounds of up to
-    // kTcdStageMats bulk copies; round 0 of the next step is issued as soon
-    // as the tensor core is done with the slice buffers.
-    const int nmat = a.Ke + 1;
-    const int nrounds = (nmat + kTcdStageMats - 1) / kTcdStageMats;
-    uint32_t tphase = 0, tissued = 0;  // rounds waited for / issued (same in every thread)
-    auto issue_round = [&](int r) {
+    // The X planes of step st reach the A slice buffer by one bulk copy, issued
+    // as soon as the previous step's last product is done with the buffer.
+    uint32_t tphase = 0, tissued = 0;  // copies waited for / issued (same in every thread)
+    auto issue_x = [&](long long st) {
         ++tissued;
         if (t.tid == 0) {
-            const int n = min(kTcdStageMats, nmat - r * kTcdStageMats);
-            mbar_expect_tx(&sh.tbar, n * kTcdMatBytes);
-            for (int i = 0; i < n; ++i)
-                bulk_g2s(SA + i * kTcdMatBytes, a.stack + (size_t)(r * kTcdStageMats + i) * 4096, kTcdMatBytes, &sh.tbar);
+            mbar_expect_tx(&sh.tbar, kTcdXBytes);
+            bulk_g2s(SA, a.xplanes + (size_t)st * kSplitXStride, kTcdXBytes, &sh.tbar);
         }
     };
-    // Step weights (k_split_weights) reach shared memory one step ahead.
-    if (t.tid < a.Ke && s1 > s0) sh.ws[0][t.tid] = a.wts[(size_t)s0 * a.Ke + t.tid];
-    if (s1 > s0) issue_round(0);
-    __syncthreads();
+    if (s1 > s0) issue_x(s0);
     for (long long st = s0; st < s1; ++st) {
-        const int wb = (int)((st - s0) & 1);
-        float4 wnext = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (t.tid < a.Ke && st + 1 < s1) wnext = a.wts[(size_t)(st + 1) * a.Ke + t.tid];
-        // ---- assembly.  Coalesced mapping: thread tid forms the complex
-        // pairs held by float4 f = 512 j + tid of a matrix (row f / 32,
-        // columns 2 (f % 32), + 1), j = 0..3, so that every warp reads 512
-        // contiguous bytes of each staged matrix.
         float X[16];
         {
-            float xrh[8], xrl[8], xih[8], xil[8], sr[8], si[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) xrl[j] = xil[j] = sr[j] = si[j] = 0.0f;
-            for (int rd = 0; rd < nrounds; ++rd) {
-                if (rd > 0) {
-                    // Every thread is done with the previous round's matrices.
-                    tc::fence_proxy_async();
-                    __syncthreads();
-                    issue_round(rd);
-                }
-                ok = tc::mbar_wait(&sh.tbar, tphase & 1, kTcdWait) && ok;
-                ++tphase;
-                const int mb = rd * kTcdStageMats, me = min(nmat, mb + kTcdStageMats);
-                for (int mm = mb; mm < me; ++mm) {
-                    const float4 *Hm = reinterpret_cast<const float4 *>(SA + (mm - mb) * kTcdMatBytes) + t.tid;
-                    float gr[8], gi[8];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const float4 v = Hm[512 * j];
-                        gr[2 * j] = v.x;
-                        gi[2 * j] = v.y;
-                        gr[2 * j + 1] = v.z;
-                        gi[2 * j + 1] = v.w;
-                    }
-                    if (mm == 0) {
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            xrh[j] = gr[j];
-                            xih[j] = gi[j];
-                        }
-                        continue;
-                    }
-                    const int m = mm - 1;
-                    const float4 w = sh.ws[wb][m];
-                    // The branches depend on the slot's weight only: uniform over the CTA.
-                    if (m < a.K) {
-                        if (w.z == 0.0f && w.w == 0.0f) {  // real weight (real control samples)
-#pragma unroll
-                            for (int j = 0; j < 8; ++j)
-                                df_mac_lazy2(xrh[j], xih[j], xrl[j], xil[j], w.x, w.y, gr[j], gi[j]);
-                        } else {
-                            const cdf wd = {{w.x, w.y}, {w.z, w.w}};
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                const cdf x = cdf_add(cdf{df_norm(xrh[j], xrl[j]), df_norm(xih[j], xil[j])},
-                                                      cdf_mul_c(wd, make_float2(gr[j], gi[j])));
-                                xrh[j] = x.re.hi;
-                                xrl[j] = x.re.lo;
-                                xih[j] = x.im.hi;
-                                xil[j] = x.im.lo;
-                            }
-                        }
-                    } else if (w.x == 0.0f) {
-                        // commutator slot with an imaginary weight i v: w h = -v h_i + i v h_r
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            sr[j] = fmaf(-w.z, gi[j], sr[j]);
-                            si[j] = fmaf(w.z, gr[j], si[j]);
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            sr[j] = fmaf(w.x, gr[j], fmaf(-w.z, gi[j], sr[j]));
-                            si[j] = fmaf(w.x, gi[j], fmaf(w.z, gr[j], si[j]));
-                        }
-                    }
-                }
-            }
-            // X in double-float into four row-padded planes (re hi, re lo, im hi,
-            // im lo) over the staging buffers, then read back in the lane layout.
-            tc::fence_proxy_async();
-            __syncthreads();
-            float *XP = reinterpret_cast<float *>(SA);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int f = 512 * j + t.tid, row = f >> 5, col = 2 * (f & 31);
-                const df r0 = df_add_f(df_norm(xrh[2 * j], xrl[2 * j]), sr[2 * j]);
-                const df r1 = df_add_f(df_norm(xrh[2 * j + 1], xrl[2 * j + 1]), sr[2 * j + 1]);
-                const df i0 = df_add_f(df_norm(xih[2 * j], xil[2 * j]), si[2 * j]);
-                const df i1 = df_add_f(df_norm(xih[2 * j + 1], xil[2 * j + 1]), si[2 * j + 1]);
-                const int o = row * kTcdPlaneLd + col;
-                *reinterpret_cast<float2 *>(XP + o) = make_float2(r0.hi, r1.hi);
-                *reinterpret_cast<float2 *>(XP + kTcdPlane + o) = make_float2(r0.lo, r1.lo);
-                *reinterpret_cast<float2 *>(XP + 2 * kTcdPlane + o) = make_float2(i0.hi, i1.hi);
-                *reinterpret_cast<float2 *>(XP + 3 * kTcdPlane + o) = make_float2(i0.lo, i1.lo);
-            }
-            __syncthreads();
-            // The next step's weights: every thread is past this step's assembly.
-            if (t.tid < a.Ke) sh.ws[wb ^ 1][t.tid] = wnext;
+            ok = tc::mbar_wait(&sh.tbar, tphase & 1, kTcdWait) && ok;
+            ++tphase;
+            const float *XP = reinterpret_cast<const float *>(SA);
             // E = c0 I + i nu_1 X in this thread's plane: E_re = c0 d - nu_1 X_im,
             // E_im = nu_1 X_re.
             {
@@ -662,7 +559,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         }
         // ---- running product E^P <- E^P + E + E E^P
         if (st == s0) {
-            if (st + 1 < s1) issue_round(0);  // the slice buffers are free again
+            if (st + 1 < s1) issue_x(st + 1);  // the slice buffers are free again
             store_ep(t.tm_ep, Eh, El);
         } else {
             {
@@ -674,7 +571,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             store_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
             nb ^= 1;
             if (!run_product(sh, t, SA, SB, kTcdHi, kTcdHi, kTcdHi - 1, false, ncommit, ok)) break;
-            if (st + 1 < s1) issue_round(0);  // the slice buffers are free again
+            if (st + 1 < s1) issue_x(st + 1);  // the slice buffers are free again
             epilogue_running(sh, t, Eh, El);
         }
     }
@@ -708,6 +605,93 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     }
 }
 
+// X_j of steps s_off .. s_off + n - 1 of the split form, in double-float, for
+// the tensor-core step kernel: X_j = H_0 + sum_m w_jm H_m with the weights of
+// k_split_weights.  Thread f of the CTA row blockIdx.x owns float4 f of every
+// expansion matrix (complex elements 2f, 2f + 1; the CTA keeps its slice of
+// the stack and the weights of its kAsmSteps steps blockIdx.y kAsmSteps, ...
+// in shared memory) and walks those steps; each element takes the same
+// operations in the same order
+// as an assembly inside the step kernel would (real weights: paired
+// double-float multiply-add; complex weights: complex double-float;
+// commutator slots: FP32 sums added at the end).  Output: four planes (re hi,
+// re lo, im hi, im lo) of 64 rows x 68 floats per step, kSplitXStride floats
+// apart.
+constexpr int kAsmSteps = 32;
+
+__global__ void __launch_bounds__(128) k_split_assemble(const __grid_constant__ SplitArgs a, float *xp,
+                                                        long long s_off, long long n) {
+    extern __shared__ float4 hs[];  // (1 + Ke) x 128 float4 of the stack, then kAsmSteps x Ke weights
+    float4 *wsa = hs + (a.Ke + 1) * 128;
+    const int f = blockIdx.x * 128 + threadIdx.x;
+    const long long sb = (long long)blockIdx.y * kAsmSteps;
+    const int ns = (int)(n - sb < kAsmSteps ? n - sb : kAsmSteps);
+    const float4 *stack4 = reinterpret_cast<const float4 *>(a.stack);
+    for (int m = 0; m <= a.Ke; ++m) hs[m * 128 + threadIdx.x] = stack4[(size_t)m * 2048 + f];
+    for (int i = threadIdx.x; i < ns * a.Ke; i += 128) wsa[i] = a.wts[(size_t)(s_off + sb) * a.Ke + i];
+    __syncthreads();
+    const int row = f >> 5, col = 2 * (f & 31);
+    for (int k = 0; k < ns; ++k) {
+        const long long s = sb + k;
+        const float4 *ws = wsa + k * a.Ke;
+        const float4 h0 = hs[threadIdx.x];
+        float xrh[2] = {h0.x, h0.z}, xih[2] = {h0.y, h0.w};
+        float xrl[2] = {0.f, 0.f}, xil[2] = {0.f, 0.f}, sr[2] = {0.f, 0.f}, si[2] = {0.f, 0.f};
+        for (int m = 0; m < a.Ke; ++m) {
+            const float4 v = hs[(m + 1) * 128 + threadIdx.x];
+            const float gr[2] = {v.x, v.z}, gi[2] = {v.y, v.w};
+            const float4 w = ws[m];
+            // The branches depend on the slot's weight only: uniform over the CTA.
+            if (m < a.K) {
+                if (w.z == 0.0f && w.w == 0.0f) {  // real weight (real control samples)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) df_mac_lazy2(xrh[j], xih[j], xrl[j], xil[j], w.x, w.y, gr[j], gi[j]);
+                } else {
+                    const cdf wd = {{w.x, w.y}, {w.z, w.w}};
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const cdf x = cdf_add(cdf{df_norm(xrh[j], xrl[j]), df_norm(xih[j], xil[j])},
+                                              cdf_mul_c(wd, make_float2(gr[j], gi[j])));
+                        xrh[j] = x.re.hi;
+                        xrl[j] = x.re.lo;
+                        xih[j] = x.im.hi;
+                        xil[j] = x.im.lo;
+                    }
+                }
+            } else if (w.x == 0.0f) {
+                // commutator slot with an imaginary weight i v: w h = -v h_i + i v h_r
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    sr[j] = fmaf(-w.z, gi[j], sr[j]);
+                    si[j] = fmaf(w.z, gr[j], si[j]);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    sr[j] = fmaf(w.x, gr[j], fmaf(-w.z, gi[j], sr[j]));
+                    si[j] = fmaf(w.x, gi[j], fmaf(w.z, gr[j], si[j]));
+                }
+            }
+        }
+        const df r0 = df_add_f(df_norm(xrh[0], xrl[0]), sr[0]);
+        const df r1 = df_add_f(df_norm(xrh[1], xrl[1]), sr[1]);
+        const df i0 = df_add_f(df_norm(xih[0], xil[0]), si[0]);
+        const df i1 = df_add_f(df_norm(xih[1], xil[1]), si[1]);
+        float *o = xp + (size_t)s * kSplitXStride + row * kTcdPlaneLd + col;
+        *reinterpret_cast<float2 *>(o) = make_float2(r0.hi, r1.hi);
+        *reinterpret_cast<float2 *>(o + kTcdPlane) = make_float2(r0.lo, r1.lo);
+        *reinterpret_cast<float2 *>(o + 2 * kTcdPlane) = make_float2(i0.hi, i1.hi);
+        *reinterpret_cast<float2 *>(o + 3 * kTcdPlane) = make_float2(i0.lo, i1.lo);
+        if (col == 62) {
+            // The row padding too, so that every 32-byte sector of the planes
+            // is written whole (no read of a partly written sector).
+#pragma unroll
+            for (int pl = 0; pl < 4; ++pl)
+                *reinterpret_cast<float4 *>(o + pl * kTcdPlane + 2) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
 // Step weights of the split form in double-float for all steps (the step
 // kernel reads them one step ahead): weight m of step s at wts[s Ke + m].
 __global__ void k_split_weights(const __grid_constant__ SplitArgs a, float4 *wts) {
@@ -733,9 +717,14 @@ bool split_tc_applies(int d, int Ke, int M) {
     return d == 64 && Ke <= kTcdMaxKe && M >= 3 && M <= kSplitMaxOrder && !split_tc_disabled();
 }
 
-cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, int *nchunks, cudaStream_t stream) {
+cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, float *xplanes, int *nchunks, cudaStream_t stream,
+                            cudaEvent_t ev0, cudaEvent_t ev1) {
     cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_split_tc),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcdSmem);
+    if (e != cudaSuccess) return e;
+    const size_t hs_bytes = sizeof(float4) * (128 * (size_t)(a.Ke + 1) + (size_t)kAsmSteps * a.Ke);
+    e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_split_assemble),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hs_bytes);
     if (e != cudaSuccess) return e;
     if (a.Ke > 0) {
         const long long n = a.P * a.Ke;
@@ -743,11 +732,27 @@ cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, int *nchunks, cudaS
         k_split_weights<<<blocks, 256, 0, stream>>>(a, const_cast<float4 *>(a.wts));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    SplitArgs b = a;
-    b.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)num_sms, a.P));
-    *nchunks = b.nchunks;
-    k_split_tc<<<b.nchunks, kTcdThreads, kTcdSmem, stream>>>(b);
-    return cudaGetLastError();
+    // Batches of up to kSplitXBatch steps: the X planes of the batch, then the
+    // step kernel over it; the chunks of successive batches follow each other.
+    int total = 0;
+    for (long long b0 = 0; b0 < a.P; b0 += kSplitXBatch) {
+        const long long nb = std::min<long long>(kSplitXBatch, a.P - b0);
+        const int gy = (int)((nb + kAsmSteps - 1) / kAsmSteps);
+        k_split_assemble<<<dim3(16, gy), 128, hs_bytes, stream>>>(a, xplanes, b0, nb);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        SplitArgs b = a;
+        b.P = nb;
+        b.xplanes = xplanes;
+        b.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)num_sms, nb));
+        b.chunks = a.chunks + (size_t)total * 4096;
+        if (ev0 && b0 == 0) cudaEventRecord(ev0, stream);
+        k_split_tc<<<b.nchunks, kTcdThreads, kTcdSmem, stream>>>(b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        total += b.nchunks;
+    }
+    if (ev1) cudaEventRecord(ev1, stream);
+    *nchunks = total;
+    return cudaSuccess;
 }
 
 int split_tc_take_faults() {
