@@ -133,3 +133,13 @@ def test_matches_simt_split_kernel(built_lib):
             outs.append(np.load(f).astype(np.complex128))
     assert relerr(outs[0], outs[1]) < TOL
     assert not np.array_equal(outs[0], outs[1])  # two different kernels ran
+
+
+def test_two_step_batches(built_lib):
+    """More steps than one batch of X planes (65536): the step kernel runs
+    once per batch and the chunk products of both batches meet in the tree.
+    Checked against the FP64 oracle on the same complex64 inputs."""
+    H0, H1, carr = problem(2, 65536 + 257, seed=13, norm0=5.0)
+    U, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
