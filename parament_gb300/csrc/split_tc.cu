@@ -608,37 +608,50 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
 // X_j of steps s_off .. s_off + n - 1 of the split form, in double-float, for
 // the tensor-core step kernel: X_j = H_0 + sum_m w_jm H_m with the weights of
 // k_split_weights.  Thread f of the CTA row blockIdx.x owns float4 f of every
-// expansion matrix (complex elements 2f, 2f + 1; the CTA keeps its slice of
-// the stack and the weights of its kAsmSteps steps blockIdx.y kAsmSteps, ...
-// in shared memory) and walks those steps; each element takes the same
-// operations in the same order
-// as an assembly inside the step kernel would (real weights: paired
-// double-float multiply-add; complex weights: complex double-float;
-// commutator slots: FP32 sums added at the end).  Output: four planes (re hi,
-// re lo, im hi, im lo) of 64 rows x 68 floats per step, kSplitXStride floats
-// apart.
+// expansion matrix (complex elements 2f, 2f + 1), keeps that slice of the
+// stack in registers (RK > 0: up to RK + 1 matrices, loops unrolled) or in
+// shared memory (RK = 0), stages the weights of the CTA's kAsmSteps steps
+// blockIdx.y kAsmSteps, ... in shared memory and walks those steps.  Each
+// element takes the same operations in the same order as an assembly inside
+// the step kernel would (real weights: paired double-float multiply-add;
+// complex weights: complex double-float; commutator slots: FP32 sums added at
+// the end).  Output: four planes (re hi, re lo, im hi, im lo) of 64 rows x 68
+// floats per step, kSplitXStride floats apart.
 constexpr int kAsmSteps = 32;
+constexpr int kAsmRegKe = 15;  // largest Ke with the stack slice in registers
 
+template <int RK>
 __global__ void __launch_bounds__(128) k_split_assemble(const __grid_constant__ SplitArgs a, float *xp,
                                                         long long s_off, long long n) {
-    extern __shared__ float4 hs[];  // (1 + Ke) x 128 float4 of the stack, then kAsmSteps x Ke weights
-    float4 *wsa = hs + (a.Ke + 1) * 128;
+    extern __shared__ float4 hs[];  // RK = 0: (1 + Ke) x 128 float4 of the stack; then kAsmSteps x Ke weights
+    const int Ke = RK > 0 ? min(a.Ke, RK) : a.Ke;
+    float4 *wsa = hs + (RK > 0 ? 0 : (Ke + 1) * 128);
     const int f = blockIdx.x * 128 + threadIdx.x;
     const long long sb = (long long)blockIdx.y * kAsmSteps;
     const int ns = (int)(n - sb < kAsmSteps ? n - sb : kAsmSteps);
     const float4 *stack4 = reinterpret_cast<const float4 *>(a.stack);
-    for (int m = 0; m <= a.Ke; ++m) hs[m * 128 + threadIdx.x] = stack4[(size_t)m * 2048 + f];
-    for (int i = threadIdx.x; i < ns * a.Ke; i += 128) wsa[i] = a.wts[(size_t)(s_off + sb) * a.Ke + i];
+    float4 hr[RK + 1];
+    if constexpr (RK > 0) {
+#pragma unroll
+        for (int m = 0; m <= RK; ++m) hr[m] = m <= Ke ? stack4[(size_t)m * 2048 + f] : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        for (int m = 0; m <= Ke; ++m) hs[m * 128 + threadIdx.x] = stack4[(size_t)m * 2048 + f];
+    }
+    for (int i = threadIdx.x; i < ns * Ke; i += 128) wsa[i] = a.wts[(size_t)(s_off + sb) * Ke + i];
     __syncthreads();
     const int row = f >> 5, col = 2 * (f & 31);
     for (int k = 0; k < ns; ++k) {
         const long long s = sb + k;
-        const float4 *ws = wsa + k * a.Ke;
-        const float4 h0 = hs[threadIdx.x];
+        const float4 *ws = wsa + k * Ke;
+        float4 h0;
+        if constexpr (RK > 0) h0 = hr[0]; else h0 = hs[threadIdx.x];
         float xrh[2] = {h0.x, h0.z}, xih[2] = {h0.y, h0.w};
         float xrl[2] = {0.f, 0.f}, xil[2] = {0.f, 0.f}, sr[2] = {0.f, 0.f}, si[2] = {0.f, 0.f};
-        for (int m = 0; m < a.Ke; ++m) {
-            const float4 v = hs[(m + 1) * 128 + threadIdx.x];
+#pragma unroll
+        for (int m = 0; m < (RK > 0 ? RK : 1 << 30); ++m) {
+            if (m >= Ke) break;
+            float4 v;
+            if constexpr (RK > 0) v = hr[m + 1]; else v = hs[(m + 1) * 128 + threadIdx.x];
             const float gr[2] = {v.x, v.z}, gi[2] = {v.y, v.w};
             const float4 w = ws[m];
             // The branches depend on the slot's weight only: uniform over the CTA.
@@ -722,9 +735,12 @@ cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, float *xplanes, int
     cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_split_tc),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcdSmem);
     if (e != cudaSuccess) return e;
-    const size_t hs_bytes = sizeof(float4) * (128 * (size_t)(a.Ke + 1) + (size_t)kAsmSteps * a.Ke);
-    e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_split_assemble),
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hs_bytes);
+    // The stack slice of an assemble thread sits in registers up to Ke = kAsmRegKe.
+    const bool asm_reg = a.Ke <= kAsmRegKe;
+    const void *asm_fn = asm_reg ? reinterpret_cast<const void *>(&k_split_assemble<kAsmRegKe>)
+                                 : reinterpret_cast<const void *>(&k_split_assemble<0>);
+    const size_t hs_bytes = sizeof(float4) * ((asm_reg ? 0 : 128 * (size_t)(a.Ke + 1)) + (size_t)kAsmSteps * a.Ke) + 16;
+    e = cudaFuncSetAttribute(asm_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hs_bytes);
     if (e != cudaSuccess) return e;
     if (a.Ke > 0) {
         const long long n = a.P * a.Ke;
@@ -738,7 +754,10 @@ cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, float *xplanes, int
     for (long long b0 = 0; b0 < a.P; b0 += kSplitXBatch) {
         const long long nb = std::min<long long>(kSplitXBatch, a.P - b0);
         const int gy = (int)((nb + kAsmSteps - 1) / kAsmSteps);
-        k_split_assemble<<<dim3(16, gy), 128, hs_bytes, stream>>>(a, xplanes, b0, nb);
+        long long off = b0, cnt = nb;
+        void *args[] = {const_cast<SplitArgs *>(&a), &xplanes, &off, &cnt};
+        e = cudaLaunchKernel(asm_fn, dim3(16, gy), dim3(128), args, hs_bytes, stream);
+        if (e != cudaSuccess) return e;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         SplitArgs b = a;
         b.P = nb;
