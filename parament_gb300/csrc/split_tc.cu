@@ -24,19 +24,20 @@
 // one real plane at a time: the accumulators of the real-stacked product put
 // Re C in tensor-memory lanes 0..63 and Im C in lanes 64..127, and each thread
 // keeps the plane of its own lane for 32 columns.  X Q = i X N comes from the
-// same slices with the A blocks swapped (ozaki.cuh).  Only the first-order
-// term mu_1 X = i nu_1 X couples the planes; the assembly leaves X_j in
-// double-float in shared memory and each thread forms its plane of mu_1 X from
-// the other plane there.
+// same A slices of X as X^2 (kept in shared memory, row scales included) with
+// the A blocks swapped (ozaki.cuh).  Only the first-order term mu_1 X =
+// i nu_1 X couples the planes: X_j arrives in double-float (k_split_assemble
+// forms it for every step) and each thread forms its plane of mu_1 X from the
+// other plane there.
 //
 // Layout of one CTA (512 threads, one per SM): shared memory holds the A
-// slices (4 x 24 KB) and the B slices (4 x 16 KB); during the assembly the
-// same 160 KB stage the expansion matrices (bulk copies, five at a time) and
-// then the planes that hand X_j to the lane layout.  Tensor memory holds the
+// slices (4 x 24 KB), the B slices (4 x 16 KB) and the A slices of X^4, X^6
+// (2 x 24 KB); at the start of a step the A slice buffer receives the planes
+// that hand X_j to the lane layout.  Tensor memory holds the
 // product levels (columns 0..255), E^P in double-float (256..383) and E of
 // the current step (384..511) while the polynomial products run.  Sixteen
-// warps hide the latency of the elementwise work (assembly, slicing,
-// epilogues) that surrounds each product; each thread owns one plane of 16
+// warps hide the latency of the elementwise work (slicing, epilogues) that
+// surrounds each product; each thread owns one plane of 16
 // columns of one row.  Every wait on the tensor core is bounded: a wait that
 // runs out stops the CTA, counts a fault and frees tensor memory.
 #include <math.h>
@@ -63,7 +64,10 @@ constexpr int kTcdG = 2;
 constexpr uint32_t kTcdWait = 1u << 24;
 constexpr size_t kTcdSA = (size_t)kTcdHi * oz::kASlice;
 constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
-constexpr size_t kTcdSmem = kTcdSA + kTcdSB + 1024;
+// The A slices of X^4, X^6 (two each) have their own buffer, so that the A
+// slices of X from the X^2 product stay for the odd part X Q.
+constexpr size_t kTcdSG = (size_t)kTcdG * oz::kASlice;
+constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdSG + 1024;
 // X_j reaches the lane layout through four planes (re hi, re lo, im hi, im
 // lo) of 64 rows padded to 68 floats (conflict-free 16-byte reads of a column
 // block by 32 consecutive rows).  k_split_assemble writes them for every step
@@ -127,6 +131,7 @@ __device__ __forceinline__ void peel8_df(const float (&hi)[8], const float (&lo)
 struct TcdShared {
     int amax[2][64], bmax[2][64];
     float rowmul[64], colmul[64];  // 2^(e - 7) of the last A rows / B columns
+    float rowmul_x[64];            // the same for the A slices of X (X^2 and X Q)
     uint64_t bar;                  // tensor-core products
     uint64_t tbar;                 // bulk copies of the X planes
     uint32_t tmem_base;
@@ -406,6 +411,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     unsigned char *SA = smem;
     unsigned char *SB = smem + kTcdSA;
+    unsigned char *SG = SB + kTcdSB;
     __shared__ TcdShared sh;
 
     const int warp = threadIdx.x >> 5;
@@ -502,6 +508,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         store_b<kTcdX2, false>(sh, SB, t, nb, X, X);
         nb ^= 1;
         if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit, ok)) break;
+        if (t.tid < 64) sh.rowmul_x[t.tid] = sh.rowmul[t.tid];
         epilogue_f<kTcdX2 - 1>(sh, t, G);
         {
             const float nu3 = (float)a.mu[3].y;
@@ -523,10 +530,10 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                 reduce_max<true, true>(sh, t, nb, G, G);
             else
                 reduce_max<true, false>(sh, t, nb, G, G);
-            store_a<kTcdG, false>(sh, SA, t, nb, G, G);
+            store_a<kTcdG, false>(sh, SG, t, nb, G, G);
             if (k == 2) store_b<kTcdG, false>(sh, SB, t, nb, G, G);
             nb ^= 1;
-            if (!(live = run_product(sh, t, SA, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok))) break;
+            if (!(live = run_product(sh, t, SG, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok))) break;
             epilogue_f<kTcdG - 1>(sh, t, G);
             const float me = (float)a.mu[2 * k].x;
             const float no = (2 * k + 1 <= M) ? (float)a.mu[2 * k + 1].y : 0.0f;
@@ -542,9 +549,9 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             store_ep(t.tm_e, Eh, El);
         }
         if (!live) break;
-        // ---- odd part X Q = i X N
-        reduce_max<true, true>(sh, t, nb, X, N);
-        store_a<kTcdX2, false>(sh, SA, t, nb, X, X);
+        // ---- odd part X Q = i X N: the A slices of X are still in SA.
+        reduce_max<false, true>(sh, t, nb, X, N);
+        if (t.tid < 64) sh.rowmul[t.tid] = sh.rowmul_x[t.tid];
         store_b<kTcdX2, false>(sh, SB, t, nb, N, N);
         nb ^= 1;
         if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, true, ncommit, ok)) break;
