@@ -293,11 +293,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
         const int wq = warp & 3, h = (warp - kTcEpi) >> 2, rl = 32 * wq + lane;
         for (int k = 0; k < nunits; ++k) {
             const TcWork wk = tc_work(g, k);
-            if (!tc::mbar_wait(&accf, (uint32_t)k & 1, kTcWaitLimit)) ok = false;
-            tc::fence_after_sync();
             const int row = wk.r0 + rl, cb = wk.c0 + 64 * h;
             const float2 *Cin = g.Cin ? g.Cin + (size_t)wk.b * g.sCin + (size_t)row * d + cb : nullptr;
             float2 *Co = g.Cout + (size_t)wk.b * g.sCout + (size_t)row * d + cb;
+            // This thread's 512 bytes of Cin move to L2 while the unit's MMAs run,
+            // so that the loads between the accumulator's arrival and release hit L2.
+            if (Cin)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) asm volatile("prefetch.global.L2 [%0];" ::"l"(Cin + 16 * i));
+            if (!tc::mbar_wait(&accf, (uint32_t)k & 1, kTcWaitLimit)) ok = false;
+            tc::fence_after_sync();
             const uint32_t acc = taddr + ((uint32_t)(32 * wq) << 16) + 64 * h;
 #pragma unroll 1
             for (int cc = 0; cc < 4; ++cc) {
