@@ -230,3 +230,35 @@ def test_tensor_core_matches_simt_gemm(built_lib):
             assert r.returncode == 0, r.stderr
             outs.append(np.load(f).astype(np.complex128))
     assert relerr(outs[0], outs[1]) < 1e-5
+
+
+def test_tensor_core_magnus_simpson(built_lib):
+    """complex64, d=256, Magnus with Simpson: the commutators [H0, H_k] and
+    [H_j, H_k] are single products (one batch item, unbatched operands) on the
+    tcgen05 GEMM, then the Clenshaw batch and the tree."""
+    rng = np.random.default_rng(256)
+    from parament_gb300.workloads import hermitian
+    H0 = hermitian(rng, 256, 5.0)
+    H1 = np.stack([hermitian(rng, 256, 1.0) for _ in range(2)])
+    carr = rng.standard_normal((2, 2 * 4 + 1))
+    U, M = run(H0, H1, list(carr), 1e-3, magnus=True, mode=oracle.SIMPSON, precision="fp32")
+    H0, H1, carr = (x.astype(np.complex64).astype(np.complex128) for x in (H0, H1, carr))
+    Uo, Mo, _, _ = oracle.equiprop(H0, H1, carr, 1e-3, magnus=True, mode=oracle.SIMPSON, single=True,
+                                   nthreads=os.cpu_count())
+    assert M == Mo
+    assert relerr(U, Uo) < TOL["fp32"]
+
+
+def test_tensor_core_d512_against_oracle(built_lib):
+    """complex64, d=512 (16 tiles of 128 x 128 complex per product): two steps
+    against the oracle, including the tree's single product."""
+    rng = np.random.default_rng(512)
+    from parament_gb300.workloads import hermitian
+    H0 = hermitian(rng, 512, 8.0)
+    H1 = hermitian(rng, 512, 1.0)[None]
+    carr = rng.standard_normal((1, 2))
+    U, M = run(H0, H1, list(carr), 1e-3, precision="fp32")
+    H0, H1, carr = (x.astype(np.complex64).astype(np.complex128) for x in (H0, H1, carr))
+    Uo, Mo, _, _ = oracle.equiprop(H0, H1, carr, 1e-3, single=True, nthreads=os.cpu_count())
+    assert M == Mo
+    assert relerr(U, Uo) < TOL["fp32"]
