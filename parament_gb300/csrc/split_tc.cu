@@ -132,6 +132,7 @@ struct TcdShared {
     int amax[2][64], bmax[2][64];
     float rowmul[64], colmul[64];  // 2^(e - 7) of the last A rows / B columns
     float rowmul_x[64];            // the same for the A slices of X (X^2 and X Q)
+    float colmul_p[64];            // column scales of the running product's B (E^P)
     uint64_t bar;                  // tensor-core products
     uint64_t tbar;                 // bulk copies of the X planes
     uint32_t tmem_base;
@@ -212,8 +213,8 @@ __device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const 
 // thread's 16 columns are contiguous within it.
 template <int S, bool DF>
 __device__ __forceinline__ void store_b(TcdShared &sh, unsigned char *SB, const TcdThread &t, int b,
-                                        const float (&hi)[16], const float (&lo)[16]) {
-    if (t.p == 0 && t.r < 16) sh.colmul[t.c0 + t.lane] = unscale_of(sh.bmax[b][t.c0 + t.lane]);
+                                        const float (&hi)[16], const float (&lo)[16], float *colmul) {
+    if (t.p == 0 && t.r < 16) colmul[t.c0 + t.lane] = unscale_of(sh.bmax[b][t.c0 + t.lane]);
     const int k = 64 * t.p + t.r;
     const int4 *cm = reinterpret_cast<const int4 *>(sh.bmax[b] + t.c0);
 #pragma unroll
@@ -238,13 +239,12 @@ __device__ __forceinline__ void store_b(TcdShared &sh, unsigned char *SB, const 
     }
 }
 
-// Makes the slices visible to the tensor core, issues one sliced product and
-// waits for it.  `ok` carries this thread's result of the previous wait; the
-// barrier before the issue combines it over the CTA, and a product is issued
-// only if every earlier wait succeeded (returns false otherwise, in every
-// thread).
-__device__ __forceinline__ bool run_product(TcdShared &sh, const TcdThread &t, unsigned char *SA, unsigned char *SB,
-                                            int sa_n, int sb_n, int lmax, bool imag, uint32_t &ncommit, bool &ok) {
+// Makes the slices visible to the tensor core and issues one sliced product.
+// `ok` carries this thread's result of the previous wait; the barrier before
+// the issue combines it over the CTA, and a product is issued only if every
+// earlier wait succeeded (returns false otherwise, in every thread).
+__device__ __forceinline__ bool issue_sliced(TcdShared &sh, const TcdThread &t, unsigned char *SA, unsigned char *SB,
+                                             int sa_n, int sb_n, int lmax, bool imag, bool ok) {
     tc::fence_proxy_async();
     tc::fence_before_sync();
     const bool all_ok = __syncthreads_and(ok) != 0;
@@ -254,9 +254,18 @@ __device__ __forceinline__ bool run_product(TcdShared &sh, const TcdThread &t, u
         oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, true);
         tc::mma_commit(&sh.bar);
     }
+    return true;
+}
+// Waits for the product issued last.
+__device__ __forceinline__ void wait_sliced(TcdShared &sh, uint32_t &ncommit, bool &ok) {
     ok = tc::mbar_wait(&sh.bar, ncommit & 1, kTcdWait);
     ++ncommit;
     tc::fence_after_sync();
+}
+__device__ __forceinline__ bool run_product(TcdShared &sh, const TcdThread &t, unsigned char *SA, unsigned char *SB,
+                                            int sa_n, int sb_n, int lmax, bool imag, uint32_t &ncommit, bool &ok) {
+    if (!issue_sliced(sh, t, SA, SB, sa_n, sb_n, lmax, imag, ok)) return false;
+    wait_sliced(sh, ncommit, ok);
     return true;
 }
 
@@ -324,7 +333,7 @@ __device__ __forceinline__ void epilogue_running(const TcdShared &sh, const TcdT
             two_sum(d0[j], d1[j] * 0.00390625f, s, e);
             e = __fadd_rn(e, __fmaf_rn(d3[j], 5.9604644775390625e-8f, d2[j] * 1.52587890625e-5f));
             df v = df_norm(s, e);
-            const float sc = rm * sh.colmul[t.c0 + 8 * h + j];
+            const float sc = rm * sh.colmul_p[t.c0 + 8 * h + j];
             v.hi *= sc;
             v.lo *= sc;
             df w = df_add(df{ph[j], pl[j]}, df{eh[8 * h + j], el[8 * h + j]});
@@ -505,7 +514,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         float N[16], G[16];
         reduce_max<true, true>(sh, t, nb, X, X);
         store_a<kTcdX2, false>(sh, SA, t, nb, X, X);
-        store_b<kTcdX2, false>(sh, SB, t, nb, X, X);
+        store_b<kTcdX2, false>(sh, SB, t, nb, X, X, sh.colmul);
         nb ^= 1;
         if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit, ok)) break;
         if (t.tid < 64) sh.rowmul_x[t.tid] = sh.rowmul[t.tid];
@@ -531,7 +540,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             else
                 reduce_max<true, false>(sh, t, nb, G, G);
             store_a<kTcdG, false>(sh, SG, t, nb, G, G);
-            if (k == 2) store_b<kTcdG, false>(sh, SB, t, nb, G, G);
+            if (k == 2) store_b<kTcdG, false>(sh, SB, t, nb, G, G, sh.colmul);
             nb ^= 1;
             if (!(live = run_product(sh, t, SG, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok))) break;
             epilogue_f<kTcdG - 1>(sh, t, G);
@@ -549,12 +558,23 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             store_ep(t.tm_e, Eh, El);
         }
         if (!live) break;
-        // ---- odd part X Q = i X N: the A slices of X are still in SA.
+        // ---- odd part X Q = i X N: the A slices of X are still in SA; the B
+        // slices of N go to SG (free after X^6).
         reduce_max<false, true>(sh, t, nb, X, N);
         if (t.tid < 64) sh.rowmul[t.tid] = sh.rowmul_x[t.tid];
-        store_b<kTcdX2, false>(sh, SB, t, nb, N, N);
+        store_b<kTcdX2, false>(sh, SG, t, nb, N, N, sh.colmul);
         nb ^= 1;
-        if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, true, ncommit, ok)) break;
+        if (!issue_sliced(sh, t, SA, SG, kTcdX2, kTcdX2, kTcdX2 - 1, true, ok)) break;
+        if (st > s0) {
+            // While the tensor core runs X Q: the B operand of the running
+            // product, E^P of the previous steps, sliced into SB (its column
+            // scales in colmul_p, apart from those of N).
+            float Ph[16], Pl[16];
+            load_ep(t.tm_ep, Ph, Pl);
+            reduce_max<false, true>(sh, t, nb, Ph, Ph);
+            store_b<kTcdHi, true>(sh, SB, t, nb, Ph, Pl, sh.colmul_p);
+        }
+        wait_sliced(sh, ncommit, ok);
         epilogue_f<kTcdX2 - 1>(sh, t, G);
         float Eh[16], El[16];
         load_ep(t.tm_e, Eh, El);
@@ -569,12 +589,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             if (st + 1 < s1) issue_x(st + 1);  // the slice buffers are free again
             store_ep(t.tm_ep, Eh, El);
         } else {
-            {
-                float Ph[16], Pl[16];
-                load_ep(t.tm_ep, Ph, Pl);
-                reduce_max<true, true>(sh, t, nb, Eh, Ph);
-                store_b<kTcdHi, true>(sh, SB, t, nb, Ph, Pl);
-            }
+            reduce_max<true, false>(sh, t, nb, Eh, Eh);
             store_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
             nb ^= 1;
             if (!run_product(sh, t, SA, SB, kTcdHi, kTcdHi, kTcdHi - 1, false, ncommit, ok)) break;
