@@ -532,7 +532,12 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             }
             store_ep(t.tm_e, Eh, El);
         }
-        // ---- higher even powers X^(2k) = X^(2k-2) X^2
+        // ---- higher even powers X^(2k) = X^(2k-2) X^2.  Their terms mu_(2k) X^(2k)
+        // are of order (h ||X||)^4 and below: they collect in FP32 (Se) and
+        // reach E together with the odd part.
+        float Se[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) Se[j] = 0.0f;
         bool live = true;
         for (int k = 2; 2 * k <= M; ++k) {
             if (k == 2)
@@ -546,16 +551,11 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             epilogue_f<kTcdG - 1>(sh, t, G);
             const float me = (float)a.mu[2 * k].x;
             const float no = (2 * k + 1 <= M) ? (float)a.mu[2 * k + 1].y : 0.0f;
-            float Eh[16], El[16];
-            load_ep(t.tm_e, Eh, El);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-                const df v = df_add_f(df{Eh[j], El[j]}, me * G[j]);
-                Eh[j] = v.hi;
-                El[j] = v.lo;
+                Se[j] = fmaf(me, G[j], Se[j]);
                 N[j] = fmaf(no, G[j], N[j]);
             }
-            store_ep(t.tm_e, Eh, El);
         }
         if (!live) break;
         // ---- odd part X Q = i X N: the A slices of X are still in SA; the B
@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         load_ep(t.tm_e, Eh, El);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            const df v = df_add_f(df{Eh[j], El[j]}, G[j]);
+            const df v = df_add_f(df_add_f(df{Eh[j], El[j]}, G[j]), Se[j]);
             Eh[j] = v.hi;
             El[j] = v.lo;
         }
