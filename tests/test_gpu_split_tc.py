@@ -143,3 +143,13 @@ def test_two_step_batches(built_lib):
     U, _ = split_equiprop(H0, H1, list(carr), 1e-3, False, oracle.NONE)
     Uo = oracle.equiprop(H0, H1, carr, 1e-3, nthreads=os.cpu_count())[0]
     assert relerr(U, Uo) < TOL
+
+
+def test_wide_expansion_magnus_k5(built_lib):
+    """Magnus with five controls: 20 expansion matrices (H_k, [H0, H_k] and the
+    pair commutators), more than the assemble kernel keeps in registers, so its
+    shared-memory form runs."""
+    H0, H1, carr = problem(5, 2 * 700 + 1, seed=41)
+    U, _ = split_equiprop(H0, H1, list(carr), 1e-3, True, oracle.SIMPSON)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, magnus=True, mode=oracle.SIMPSON, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
