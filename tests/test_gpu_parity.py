@@ -212,12 +212,13 @@ def test_tensor_core_large_dimension(built_lib, d, P):
     assert relerr(U, Uo) < TOL["fp32"]
 
 
-def test_tensor_core_matches_simt_gemm(built_lib):
-    """d=512: the tcgen05 path and the SIMT GEMM path (tensor cores disabled
-    through PARAMENT_DISABLE_TENSOR_CORES in a child process) agree."""
+@pytest.mark.parametrize("d,K,steps", [(512, 8, 5), (1024, 4, 2)])
+def test_tensor_core_matches_simt_gemm(built_lib, d, K, steps):
+    """d=512 and d=1024: the tcgen05 path and the SIMT GEMM path (tensor cores
+    disabled through PARAMENT_DISABLE_TENSOR_CORES in a child process) agree."""
     code = ("import sys, numpy as np, parament_gb300 as p\n"
             "from parament_gb300 import workloads\n"
-            "w = workloads.large_dense(d=512, K=8, steps=5)\n"
+            f"w = workloads.large_dense(d={d}, K={K}, steps={steps})\n"
             "c = p.Parament('fp32'); c.set_hamiltonian(w['H0'], *w['H1'])\n"
             "np.save(sys.argv[1], c.equiprop(w['dt'], *w['carr']))\n")
     import tempfile
