@@ -281,6 +281,117 @@ __global__ void k_c128_to_c64(const double2 *src, float2 *dst, int n) {
     if (i < n) dst[i] = make_float2((float)src[i].x, (float)src[i].y);
 }
 
+// The chunk products of the split form multiplied in order, in double-float.
+// Each product keeps about 2^-44 relative.  FP64 runs at 1/64 of the FP32 rate
+// on this GPU, and double-float is far more than the form's 1e-6 needs.
+//
+// Level: W_i = U_(2i) + (U_(2i+1) - I) U_(2i), with the later factor on the
+// left (the pairing of src/cuda/parament.cpp:657-718).  An odd leftover moves
+// to the end unchanged.  One CTA forms one 16 x 16 tile of one W_i; the CTAs
+// of index `pairs` copy the leftover.  Elements are float4 (re hi, re lo,
+// im hi, im lo); IN = double2 reads the complex128 chunk products of the step
+// kernels.
+__device__ __forceinline__ float4 to_df4(double2 v) {
+    const df r = df_from(v.x), i = df_from(v.y);
+    return make_float4(r.hi, r.lo, i.hi, i.lo);
+}
+__device__ __forceinline__ float4 to_df4(float4 v) { return v; }
+
+// (hi, lo) += x y for double-float x, y, without renormalising: the product's
+// rounding error joins lo with the rounding of the sum.
+__device__ __forceinline__ void df_mac_dd(float &hi, float &lo, float xh, float xl, float yh, float yl) {
+    const float p = __fmul_rn(xh, yh);
+    float e = __fmaf_rn(xh, yh, -p);
+    e = __fmaf_rn(xh, yl, e);
+    e = __fmaf_rn(xl, yh, e);
+    float s, t;
+    two_sum(hi, p, s, t);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(t, e));
+}
+
+template <class IN>
+__global__ void __launch_bounds__(256) k_tree_df(const IN *__restrict__ in, float4 *__restrict__ out, int d,
+                                                 long long pairs) {
+    __shared__ float4 As[16][kSmallMaxDim + 1];  // rows r0..r0+15 of A - I
+    __shared__ float4 Bs[kSmallMaxDim][17];      // columns c0..c0+15 of B
+    const int tiles = (d + 15) / 16;
+    const int r0 = (blockIdx.x / tiles) * 16, c0 = (blockIdx.x % tiles) * 16;
+    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15, r = r0 + ty, c = c0 + tx;
+    const long long pr = blockIdx.y;
+    const size_t dd = (size_t)d * d;
+    if (pr == pairs) {  // the odd leftover
+        if (r < d && c < d) out[pr * dd + (size_t)r * d + c] = to_df4(in[2 * pr * dd + (size_t)r * d + c]);
+        return;
+    }
+    const IN *A = in + (2 * pr + 1) * dd, *B = in + 2 * pr * dd;
+    for (int i = threadIdx.x; i < 16 * d; i += 256) {
+        const int rr = r0 + i / d, k = i % d;
+        float4 v = rr < d ? to_df4(A[(size_t)rr * d + k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (rr == k) {
+            // A - I: the hi part of a diagonal entry near 1 loses the 1 exactly.
+            const df t = df_add_f(df{v.x, v.y}, -1.0f);
+            v.x = t.hi;
+            v.y = t.lo;
+        }
+        As[i / d][k] = v;
+    }
+    for (int i = threadIdx.x; i < 16 * d; i += 256) {
+        const int k = i / 16, cc = c0 + i % 16;
+        Bs[k][i % 16] = cc < d ? to_df4(B[(size_t)k * d + cc]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    if (r >= d || c >= d) return;
+    const float4 b0 = to_df4(B[(size_t)r * d + c]);
+    float rh = b0.x, rl = b0.y, ih = b0.z, il = b0.w;
+    for (int k = 0; k < d; ++k) {
+        const float4 a = As[ty][k], b = Bs[k][tx];
+        df_mac_dd(rh, rl, a.x, a.y, b.x, b.y);
+        df_mac_dd(rh, rl, -a.z, -a.w, b.z, b.w);
+        df_mac_dd(ih, il, a.x, a.y, b.z, b.w);
+        df_mac_dd(ih, il, a.z, a.w, b.x, b.y);
+    }
+    const df re = df_norm(rh, rl), im = df_norm(ih, il);
+    out[pr * dd + (size_t)r * d + c] = make_float4(re.hi, re.lo, im.hi, im.lo);
+}
+
+__global__ void k_df_to_c64(const float4 *src, float2 *dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = make_float2(__fadd_rn(src[i].x, src[i].y), __fadd_rn(src[i].z, src[i].w));
+}
+
+// Product of n chunk products (complex128, in order of time) into the complex64
+// output; bufa, bufb hold at least ceil(n / 2) d x d double-float matrices
+// (bufa may be the chunk buffer itself).
+static cudaError_t tree_df(int d, const double2 *chunks, long long n, float4 *bufa, float4 *bufb, float2 *out,
+                           cudaStream_t stream, int *levels) {
+    *levels = 0;
+    const int dd = d * d, tiles = (d + 15) / 16;
+    if (n == 1) {
+        k_c128_to_c64<<<(dd + 255) / 256, 256, 0, stream>>>(chunks, out, dd);
+        return cudaGetLastError();
+    }
+    long long remain = n;
+    const float4 *cur = nullptr;
+    float4 *dst = bufb;
+    while (remain > 1) {
+        const long long pairs = remain / 2;
+        dim3 grid(tiles * tiles, (unsigned)(pairs + remain % 2));
+        if (cur == nullptr)
+            k_tree_df<double2><<<grid, 256, 0, stream>>>(chunks, dst, d, pairs);
+        else
+            k_tree_df<float4><<<grid, 256, 0, stream>>>(cur, dst, d, pairs);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        ++*levels;
+        remain = pairs + remain % 2;
+        cur = dst;
+        dst = (dst == bufb) ? bufa : bufb;
+    }
+    k_df_to_c64<<<(dd + 255) / 256, 256, 0, stream>>>(cur, out, dd);
+    return cudaGetLastError();
+}
+
 // Complex64 stack from the FP64 stack (round to nearest).
 __global__ void k_split_stack(const double2 *src, float2 *dst, long long n) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -483,12 +594,8 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
     }
     int levels = 0;
     if (e == cudaSuccess)
-        e = tree_product(true, d, c->chunks.ptr, a.nchunks, c->work.ptr, c->aux.ptr, stream, c->num_sms, &levels);
-    if (e == cudaSuccess) {
-        k_c128_to_c64<<<(int)((dd + 255) / 256), 256, 0, stream>>>(static_cast<const double2 *>(c->aux.ptr),
-                                                                   static_cast<float2 *>(d_out), (int)dd);
-        e = cudaGetLastError();
-    }
+        e = tree_df(d, static_cast<const double2 *>(c->chunks.ptr), a.nchunks, static_cast<float4 *>(c->chunks.ptr),
+                    static_cast<float4 *>(c->work.ptr), static_cast<float2 *>(d_out), stream, &levels);
     // Step kernels (tensor form: step weights, then X planes and step kernel
     // per batch), the tree levels and the final conversion.
     const long long batches = (P + kSplitXBatch - 1) / kSplitXBatch;
