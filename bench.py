@@ -11,7 +11,7 @@ Forms measured:
   plain_c128 : the reference scheme in complex128 (FP64 arithmetic)
   plain_c64  : the reference scheme in complex64
   split_c64  : the split-precision complex64 form (double-float low-order
-               terms, FP64 tree top), when the library provides it
+               terms and chunk tree), when the library provides it
 The headline form is the fastest form whose relative Frobenius error against
 the FP64 result is <= 1e-6.
 
@@ -603,7 +603,7 @@ def run_ours(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": round(ms_per, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": {"plain_c128": "c128 (f64)", "plain_c64": "c64 (f32)",
-                  "split_c64": "c64 (f32 + double-float low orders, f64 tree top)"}[head],
+                  "split_c64": "c64 (f32 + double-float low orders and tree)"}[head],
         "data": "synthetic (seeded Hermitian H0/H_k, sinusoid+noise controls)",
         "config": {"workload": "magnus_d64_K4_simpson_65536steps", "d": d, "K": K, "steps": P,
                    "samples_per_control": int(w["carr"].shape[1]), "dt": w["dt"], "norm_H0": 10.0,
