@@ -416,8 +416,9 @@ __device__ __forceinline__ void df_mac_lazy2(float &hi0, float &hi1, float &lo0,
 
 __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_constant__ SplitArgs a) {
     extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem =
-        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    // 1024-byte alignment by pointer arithmetic on the shared array, so that the
+    // compiler keeps every access derived from it in the shared state space.
+    unsigned char *smem = smem_raw + ((1024u - (tc::smem_addr(smem_raw) & 1023u)) & 1023u);
     unsigned char *SA = smem;
     unsigned char *SB = smem + kTcdSA;
     unsigned char *SG = SB + kTcdSB;
