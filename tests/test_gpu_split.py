@@ -106,3 +106,17 @@ def test_split_mode_only_for_fp32(built_lib):
     with parament.Parament("fp64") as ctx:
         with pytest.raises(ValueError):
             ctx.set_precision_mode("split")
+
+
+@pytest.mark.parametrize("d", [24, 40])
+def test_split_partial_tiles(built_lib, d):
+    """Dimensions that are not multiples of 16 (the SIMT split kernel and the
+    double-float chunk tree with partial 16 x 16 tiles), Magnus with Simpson."""
+    from parament_gb300.workloads import hermitian
+    rng = np.random.default_rng(d)
+    H0 = c64(hermitian(rng, d, 5.0))
+    H1 = c64(np.stack([hermitian(rng, d, 1.0) for _ in range(2)]))
+    carr = c64(rng.standard_normal((2, 2 * 500 + 1)))
+    U, _ = run_split(H0, H1, list(carr), 1e-3, True, oracle.SIMPSON)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, magnus=True, mode=oracle.SIMPSON, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < 1e-6
