@@ -3,8 +3,8 @@
 // Same polynomial and the same chunked running product as k_split_steps
 // (split.cu): U_j = I + E_j with the reference's Chebyshev-Bessel polynomial
 // regrouped by powers of X_j, each CTA multiplying its chunk of consecutive
-// steps into E^P in double-float, the chunk products combined by the FP64
-// tree.  What changes is where the products run: every d^3 product is a
+// steps into E^P in double-float, the chunk products combined by the
+// double-float tree (split.cu).  What changes is where the products run: every d^3 product is a
 // sliced bf16 product on the tensor cores (ozaki.cuh) whose levels accumulate
 // exactly in tensor memory.
 //
@@ -31,14 +31,15 @@
 // other plane there.
 //
 // Layout of one CTA (512 threads, one per SM): shared memory holds the A
-// slices (4 x 24 KB), the B slices (4 x 16 KB) and the A slices of X^4, X^6
-// (2 x 24 KB); at the start of a step the A slice buffer receives the planes
-// that hand X_j to the lane layout.  Tensor memory holds the
-// product levels (columns 0..255), E^P in double-float (256..383) and E of
-// the current step (384..511) while the polynomial products run.  Sixteen
-// warps hide the latency of the elementwise work (slicing, epilogues) that
-// surrounds each product; each thread owns one plane of 16
-// columns of one row.  Every wait on the tensor core is bounded: a wait that
+// slices (4 x 24 KB), the B slices (4 x 16 KB) and a third buffer (2 x 24 KB)
+// for the A slices of X^4, X^6 and then the B slices of N; at the start of a
+// step the A slice buffer receives the planes that hand X_j to the lane
+// layout.  Tensor memory holds the product levels (columns 0..255), E^P in
+// double-float (256..383) and E of the current step (384..511) while the
+// polynomial products run.  Sixteen warps hide the latency of the elementwise
+// work (slicing, epilogues) that surrounds each product; each thread owns one
+// plane of 16 columns of one row.  While the tensor core runs X Q, the threads
+// slice E^P, the B operand of the running product.  Every wait on the tensor core is bounded: a wait that
 // runs out stops the CTA, counts a fault and frees tensor memory.
 #include <math.h>
 #include <stdlib.h>
