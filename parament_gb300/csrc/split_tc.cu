@@ -65,8 +65,9 @@ constexpr int kTcdG = 2;
 constexpr uint32_t kTcdWait = 1u << 24;
 constexpr size_t kTcdSA = (size_t)kTcdHi * oz::kASlice;
 constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
-// The A slices of X^4, X^6 (two each) have their own buffer, so that the A
-// slices of X from the X^2 product stay for the odd part X Q.
+// A third slice buffer takes the A slices of X^4, X^6 (two each) and then the
+// B slices of N (three), so that the A slices of X from the X^2 product stay
+// for the odd part X Q and the B buffer is free for E^P while X Q runs.
 constexpr size_t kTcdSG = (size_t)kTcdG * oz::kASlice;
 constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdSG + 1024;
 // X_j reaches the lane layout through four planes (re hi, re lo, im hi, im
