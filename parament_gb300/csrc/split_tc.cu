@@ -643,6 +643,10 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
 // the end).  Output: four planes (re hi, re lo, im hi, im lo) of 64 rows x 68
 // floats per step, kSplitXStride floats apart.
 constexpr int kAsmSteps = 32;
+// Shared memory of k_split_assemble at the largest Ke: its stack slice and the
+// weights of its steps.
+static_assert(sizeof(float4) * (128 * (kTcdMaxKe + 1) + kAsmSteps * kTcdMaxKe) + 16 <= 232448,
+              "k_split_assemble exceeds 227 KB of shared memory");
 constexpr int kAsmRegKe = 15;  // largest Ke with the stack slice in registers
 
 template <int RK>
