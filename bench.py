@@ -52,7 +52,10 @@ def parse():
                    choices=["split_c64", "plain_c64", "plain_c128", "large_dense_d512", "vjp_d32", "ensemble"],
                    help="run one form twice (for ncu captures) and exit")
     p.add_argument("--forms", default="plain_c128,plain_c64,split_c64",
-                   help="comma-separated forms to measure (plain_c128 is the error reference)")
+                   help="comma-separated forms to measure")
+    p.add_argument("--large-c128-steps", type=int, default=4,
+                   help="steps of the d=1024 complex128 workload to time (2048: the whole workload, ~3 min)")
+    p.add_argument("--no-scipy-baseline", action="store_true")
     return p.parse_args()
 
 
@@ -192,6 +195,14 @@ def flops_per_step(d, M, Ke, form):
     if form == "split_c64":
         return gemm * split_products(M)
     return gemm * M + 8.0 * Ke * d * d
+
+
+def algorithmic_flops_per_step(d, M, Ke):
+    """Algorithmic flops of one time step as the reference scheme counts them:
+    M + 1 complex d^3 products (M Clenshaw products and one product of the
+    tree) and the assembly, Ke complex multiply-adds per element:
+    8 d^3 (M + 1) + 8 Ke d^2, with M the FP64 order table's order."""
+    return 8.0 * d ** 3 * (M + 1) + 8.0 * Ke * d * d
 
 
 def split_products(M):
@@ -369,78 +380,147 @@ def ensemble_block(torch, parament, K_steps, W_steps):
     return out
 
 
-def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, steps=1024, err_steps=256):
-    """Large dense workload, complex64 d=512, K=8, ||H0|| = 20, smooth
-    8-mode Fourier controls, on a 1024-step prefix of the 8192 steps: the
-    tcgen05 3xTF32 GEMM path (kernel k_tc_cgemm).  The error column compares
-    the complex64 result with the complex128 one on a 256-step prefix."""
-    from parament_gb300 import workloads
-    w = workloads.large_dense(d=512, K=8, steps=steps)
-    ctx = parament.Parament("fp32")
-    ctx.set_hamiltonian(w["H0"], *w["H1"])
-    carr = torch.tensor(w["carr"], dtype=torch.complex64, device="cuda")
-    out = torch.empty((512, 512), dtype=torch.complex64, device="cuda")
+def time_device(torch, ctx, w, carr, out, stream, K_steps, W_steps, flush=None):
+    """Mean device time (ms) of equiprop_device over K_steps after W_steps."""
     with torch.cuda.stream(stream):
         for _ in range(W_steps):
             ctx.equiprop_device(w["dt"], carr, out, stream)
         stream.synchronize()
         ts = []
         for _ in range(K_steps):
-            flush.zero_()
+            if flush is not None:
+                flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
             ctx.equiprop_device(w["dt"], carr, out, stream)
             e.record(stream)
             ts.append((s, e))
         stream.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in ts) / len(ts)
+    return sum(a.elapsed_time(b) for a, b in ts) / len(ts)
+
+
+def oracle_prefix_error(parament, w, precision, nsteps):
+    """The first nsteps steps of a large workload on the GPU against the oracle
+    (complex64 contexts on the complex64-rounded inputs, against the oracle's
+    complex64-context arithmetic)."""
+    import oracle
+    H0, H1, c = w["H0"], w["H1"], w["carr"][:, :nsteps]
+    if precision == "fp32":
+        H0, H1, c = (x.astype(np.complex64).astype(np.complex128) for x in (H0, H1, c))
+    with parament.Parament(precision) as ctx:
+        ctx.set_hamiltonian(H0, *H1)
+        U = ctx.equiprop(w["dt"], *c).astype(np.complex128)
+    Uo = oracle.equiprop(H0, H1, c, w["dt"], single=(precision == "fp32"), nthreads=os.cpu_count() or 1)[0]
+    return float(np.linalg.norm(U - Uo) / np.linalg.norm(Uo))
+
+
+def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, err_steps=12):
+    """Large dense workload, complex64 d=512, K=8, ||H0|| = 20, smooth 8-mode
+    Fourier controls, all 8192 steps (steps x d^2 = 2^31): the tcgen05 3xTF32
+    GEMM path (kernel k_tc_cgemm).  The error column compares a prefix with
+    the oracle."""
+    from parament_gb300 import workloads
+    w = workloads.large_dense(d=512, K=8, steps=8192)
+    steps = w["P"]
+    ctx = parament.Parament("fp32")
+    ctx.set_hamiltonian(w["H0"], *w["H1"])
+    carr = torch.tensor(w["carr"], dtype=torch.complex64, device="cuda")
+    out = torch.empty((512, 512), dtype=torch.complex64, device="cuda")
+    ms = time_device(torch, ctx, w, carr, out, stream, K_steps, W_steps, flush)
     M = ctx.last_iteration_cycles
     ctx.destroy()
     flops = steps * (M + 1) * 8.0 * 512 ** 3
-    # complex64 against complex128 on the same (complex64-rounded) inputs
-    we = workloads.large_dense(d=512, K=8, steps=err_steps)
-    H0, H1, ce = (we[k].astype(np.complex64).astype(np.complex128) for k in ("H0", "H1", "carr"))
-    Us = []
-    for prec in ("fp32", "fp64"):
-        with parament.Parament(prec) as c:
-            c.set_hamiltonian(H0, *H1)
-            Us.append(c.equiprop(we["dt"], *ce).astype(np.complex128))
-    err = float(np.linalg.norm(Us[0] - Us[1]) / np.linalg.norm(Us[1]))
-    return {"workload": f"large_dense d=512 K=8 complex64, first {steps} steps", "M": M, "ms": round(ms, 3),
+    return {"workload": f"large_dense d=512 K=8 complex64, all {steps} steps", "M": M, "ms": round(ms, 3),
             "steps_per_s": round(steps / (ms * 1e-3), 1), "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
             "kernel": "k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)",
-            "rel_err_vs_fp64": err, "rel_err_steps": err_steps,
+            "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, "fp32", err_steps),
+            "rel_err_prefix_steps": err_steps,
             "scheme": "the reference's plain complex64 scheme (fp32 order table)"}
 
 
-def large_dense_c128_block(torch, parament, K_steps, W_steps, stream, steps=4):
+def large_dense_c128_block(torch, parament, K_steps, W_steps, stream, steps=4, err_steps=3):
     """Large dense complex128 workload, d=1024, K=4, ||H0|| = 20: the first
-    `steps` of its 2048 steps on the FP64 GEMM path (k_gemm, FP64 pipe)."""
+    `steps` of its 2048 steps (all of them for steps = 2048) on the FP64 GEMM
+    path (k_gemm, FP64 pipe); a prefix is checked against the oracle."""
     from parament_gb300 import workloads
     w = workloads.large_dense(d=1024, K=4, steps=steps)
     ctx = parament.Parament("fp64")
     ctx.set_hamiltonian(w["H0"], *w["H1"])
     carr = torch.tensor(w["carr"], dtype=torch.complex128, device="cuda")
     out = torch.empty((1024, 1024), dtype=torch.complex128, device="cuda")
-    with torch.cuda.stream(stream):
-        for _ in range(W_steps):
-            ctx.equiprop_device(w["dt"], carr, out, stream)
-        stream.synchronize()
-        ts = []
-        for _ in range(K_steps):
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s.record(stream)
-            ctx.equiprop_device(w["dt"], carr, out, stream)
-            e.record(stream)
-            ts.append((s, e))
-        stream.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in ts) / len(ts)
+    ms = time_device(torch, ctx, w, carr, out, stream, K_steps, W_steps)
     M = ctx.last_iteration_cycles
     ctx.destroy()
     flops = steps * (M + 1) * 8.0 * 1024 ** 3
-    return {"workload": f"large_dense d=1024 K=4 complex128, first {steps} of 2048 steps", "M": M,
+    return {"workload": f"large_dense d=1024 K=4 complex128, {steps} of 2048 steps", "M": M,
             "ms": round(ms, 3), "steps_per_s": round(steps / (ms * 1e-3), 2),
-            "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 3), "kernel": "k_gemm (FP64 pipe)"}
+            "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 3), "kernel": "k_gemm (FP64 pipe)",
+            "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, "fp64", min(err_steps, steps)),
+            "rel_err_prefix_steps": min(err_steps, steps)}
+
+
+def plain_d16_block(torch, parament, K_steps, W_steps, flush, stream, lib_peaks):
+    """Plain equiprop: d=16, K=2, 4096 steps, complex128, NONE quadrature (the
+    reference's CPU-runnable case).  Device time of the fused step kernel and
+    the whole call, FP64-pipe roofline against the measured cuBLAS DGEMM rate,
+    end to end through Parament_equiprop_fp64 with host buffers, and the error
+    against the oracle over all steps."""
+    import oracle
+    from parament_gb300 import workloads
+    w = workloads.plain_d16()
+    P = w["P"]
+    ctx = parament.Parament("fp64")
+    ctx.set_hamiltonian(w["H0"], *w["H1"])
+    lib = parament.paramentlib.lib
+    lib.Parament_setKernelTiming_fp64(ctx._handle, 1)
+    carr = torch.tensor(w["carr"], dtype=torch.complex128, device="cuda")
+    out = torch.empty((16, 16), dtype=torch.complex128, device="cuda")
+    ms = time_device(torch, ctx, w, carr, out, stream, max(K_steps, 20), W_steps, flush)
+    kms = float(lib.Parament_lastKernelMs_fp64(ctx._handle))
+    launches = int(lib.Parament_lastLaunchCount_fp64(ctx._handle))
+    M = ctx.last_iteration_cycles
+    U = out.cpu().numpy()
+    host = [np.ascontiguousarray(r) for r in w["carr"]]
+    ctx.equiprop(w["dt"], *host)
+    e2e = []
+    for _ in range(max(K_steps, 20)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.equiprop(w["dt"], *host)
+        e2e.append(time.perf_counter() - t0)
+    ctx.destroy()
+    Uo = oracle.equiprop(w["H0"], w["H1"], w["carr"], w["dt"], nthreads=os.cpu_count() or 1)[0]
+    fl = algorithmic_flops_per_step(16, M, 2) * P
+    e2e_s = statistics.median(e2e)
+    return {"workload": "plain_d16_K2_none_4096steps complex128", "M": M, "ms_per_prop": round(ms, 4),
+            "steps_per_s": round(P / (ms * 1e-3), 1), "kernel": "k_small_steps<double> + tree",
+            "kernel_ms": round(kms, 4), "launches": launches,
+            "roofline": {"bound": "fp64 pipe", "achieved_tflops": round(fl / (kms * 1e-3) / 1e12, 4),
+                         "peak_tflops": lib_peaks["fp64_gemm_tflops"],
+                         "frac": round(fl / (kms * 1e-3) / 1e12 / lib_peaks["fp64_gemm_tflops"], 4),
+                         "peak_source": "cuBLAS DGEMM 8192^3 measured in this run",
+                         "flops_rule": f"8 d^3 (M+1) + 8 K d^2 per step, M = {M}"},
+            "e2e": {"value": round(P / e2e_s, 1), "unit": UNIT, "h2d_bytes_per_step": int(w["carr"].size * 16),
+                    "d2h_bytes_per_step": 16 * 16 * 16, "api": "Parament_equiprop_fp64 (host buffers)"},
+            "rel_err_vs_oracle": float(np.linalg.norm(U - Uo) / np.linalg.norm(Uo))}
+
+
+def scipy_block(w16, w64):
+    """The NumPy/SciPy FP64 expm-product of the same scheme on the host cores:
+    one process (one BLAS thread) and one process per core over contiguous
+    chunks.  d=16: all 4096 steps; d=64 Magnus: a bounded prefix."""
+    import oracle
+    n = os.cpu_count() or 1
+    out = {"cores": n, "method": "scipy.linalg.expm(-1j h X_j) per step, ordered product, FP64"}
+    for name, w, magnus, mode, cap1, capn in (
+            ("plain_d16_4096steps", w16, False, oracle.NONE, None, None),
+            ("magnus_d64_65536steps", w64, True, oracle.SIMPSON, 4000, 4000 * n)):
+        r1 = oracle.scipy_baseline(w["H0"], w["H1"], w["carr"], w["dt"], magnus, mode, steps=cap1, procs=1)
+        rn = oracle.scipy_baseline(w["H0"], w["H1"], w["carr"], w["dt"], magnus, mode, steps=capn, procs=n)
+        out[name] = {"single_core_steps_per_s": round(r1[0], 1), "single_core_sample_steps": r1[1],
+                     "all_cores_steps_per_s": round(rn[0], 1), "all_cores_sample_steps": rn[1]}
+    return out
 
 
 def cpu_baseline(w, target_s=10.0):
@@ -523,7 +603,17 @@ def run_ours(args, rank, world, local):
             res[f] = run_form(torch, parament, w, f, args.steps, args.warmup, flush, stream)
         except (ValueError, RuntimeError) as e:
             res[f] = {"error": str(e)}
-    ref = res["plain_c128"]["U"]
+    # Errors against the oracle (the FP64 C restatement, all host threads)
+    # over all steps of the workload; the plain complex64 form also against
+    # the oracle's complex64-context arithmetic (its parity bar).
+    import oracle
+    Uo = oracle.equiprop(w["H0"], w["H1"], w["carr"], w["dt"], magnus=True, mode=oracle.SIMPSON,
+                         nthreads=os.cpu_count() or 1)[0]
+    Uo32 = None
+    if "plain_c64" in res and "error" not in res["plain_c64"]:
+        Uo32 = oracle.equiprop(w["H0"], w["H1"], w["carr"], w["dt"], magnus=True, mode=oracle.SIMPSON, single=True,
+                               nthreads=os.cpu_count() or 1)[0]
+    gpu128 = res["plain_c128"].get("U")
     summary = {}
     for f, r in res.items():
         if "error" in r:
@@ -531,8 +621,13 @@ def run_ours(args, rank, world, local):
             continue
         ms = sum(r["ms"]) / len(r["ms"])
         summary[f] = {"steps_per_s": round(P / (ms * 1e-3), 1), "ms_per_prop": round(ms, 4),
-                      "rel_err_vs_fp64": float(np.linalg.norm(r["U"] - ref) / np.linalg.norm(ref)),
+                      "rel_err_vs_fp64": float(np.linalg.norm(r["U"] - Uo) / np.linalg.norm(Uo)),
                       "M": r["M"], "kernel_ms": round(sum(r["kernel_ms"]) / len(r["kernel_ms"]), 4)}
+        if gpu128 is not None and f != "plain_c128":
+            summary[f]["rel_err_vs_gpu_c128"] = float(np.linalg.norm(r["U"] - gpu128) / np.linalg.norm(gpu128))
+        if f == "plain_c64" and Uo32 is not None:
+            summary[f]["rel_err_vs_oracle_c64_context"] = float(np.linalg.norm(r["U"] - Uo32) /
+                                                                 np.linalg.norm(Uo32))
     ok = [f for f in forms if f in summary and "steps_per_s" in summary[f] and
           summary[f]["rel_err_vs_fp64"] <= 1e-6]
     head = max(ok, key=lambda f: summary[f]["steps_per_s"])
@@ -584,23 +679,29 @@ def run_ours(args, rank, world, local):
     d, K = 64, 4
     Ke = 2 * K + K * (K - 1) // 2
     M = r["M"]
+    hn = oracle.onenorm(w["H0"]) + sum(oracle.onenorm(h) for h in w["H1"])
+    M64 = oracle.select_cycles(hn, 2 * w["dt"], fp64=True)
     kms = sum(r["kernel_ms"]) / len(r["kernel_ms"])
-    fl = flops_per_step(d, M, Ke, head) * P
+    fl = algorithmic_flops_per_step(d, M64, Ke) * P
     achieved = fl / (kms * 1e-3) / 1e12
     pipe_peak = lib_peaks["fp64_gemm_tflops"] if head == "plain_c128" else lib_peaks["fp32_gemm_tflops"]
     pipe_rate = achieved
-    issued = None
+    issued = own = None
     if head == "split_c64":
-        # Issued tensor work: bf16 slice products of the real-stacked form
-        # (M = 128, N = 64, K = 128 real: 2 * 128 * 64 * 128 = 8 d^3 flop each),
-        # against the bf16 dense peak.
+        # The split form's own product count (X^2, X^4 .. X^(M-1), X Q, the
+        # running product) and the bf16 slice products it issues (real-stacked
+        # M = 128, N = 64, K = 128: 8 d^3 flop each), against the bf16 peak.
+        own = flops_per_step(d, M, Ke, head) * P / (kms * 1e-3) / 1e12
         issued = split_slice_products(M) * 8.0 * d ** 3 * P / (kms * 1e-3) / 1e12
         pipe_peak, pipe_rate = peaks["bf16_tflops"], issued
-    traffic = None
+    traffic, traffic_src = None, None
     tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(head)
+            tj = json.load(f)
+        if head in tj:
+            traffic = tj[head]
+            traffic_src = tj.get("source")
     e2e_s = sum(r["e2e_s"]) / len(r["e2e_s"])
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -619,9 +720,14 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(r["launches"]) * args.steps,
         "roofline": {"bound": "tensor", "achieved": round(achieved, 3), "peak": peaks["bf16_tflops"],
                      "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 5), "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_source": f"{peak_src} bf16 dense (MEASURED_PEAKS.json)",
                      "kernel": "k_small_steps" if head != "split_c64" else "k_split_tc",
-                     "algorithmic_flops_per_launch": fl, "kernel_ms": round(kms, 4),
+                     "algorithmic_flops_per_launch": fl,
+                     "algorithmic_flops_rule": f"8 d^3 (M+1) + 8 Ke d^2 per step, M = {M64} (FP64 order table), "
+                                               f"Ke = {Ke}",
+                     "kernel_ms": round(kms, 4),
+                     "own_products_tflops": round(own, 2) if own else None,
                      "issued_bf16_tflops": round(issued, 2) if issued else None,
                      "issued_bf16_frac": round(issued / peaks["bf16_tflops"], 4) if issued else None,
                      "pipe": "fp64" if head == "plain_c128" else ("tensor (bf16 slices)" if head == "split_c64" else "fp32"),
@@ -636,11 +742,17 @@ def run_ours(args, rank, world, local):
     except (ValueError, RuntimeError) as e:
         line["grape"] = {"error": str(e)}
     try:
+        line["plain_d16"] = plain_d16_block(torch, parament, args.steps, args.warmup, flush, stream, lib_peaks)
+    except (ValueError, RuntimeError) as e:
+        line["plain_d16"] = {"error": str(e)}
+    try:
         line["large_dense"] = large_dense_block(torch, parament, args.steps, args.warmup, flush, stream)
     except (ValueError, RuntimeError) as e:
         line["large_dense"] = {"error": str(e)}
     try:
-        line["large_dense_c128"] = large_dense_c128_block(torch, parament, min(args.steps, 2), 1, stream)
+        n128 = args.large_c128_steps
+        line["large_dense_c128"] = large_dense_c128_block(torch, parament, 1 if n128 > 64 else min(args.steps, 2),
+                                                          0 if n128 > 64 else 1, stream, steps=n128)
     except (ValueError, RuntimeError) as e:
         line["large_dense_c128"] = {"error": str(e)}
     if not args.no_ensemble:
@@ -651,6 +763,8 @@ def run_ours(args, rank, world, local):
     if not args.no_cpu_baseline:
         base, S, t = cpu_baseline(w)
         line["cpu_baseline"] = base
+    if not args.no_scipy_baseline:
+        line["cpu_baseline_scipy"] = scipy_block(workloads.plain_d16(), w)
     print(json.dumps(line), flush=True)
 
 

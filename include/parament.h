@@ -58,7 +58,7 @@ typedef enum Parament_ErrorCode {
     PARAMENT_STATUS_NO_HAMILTONIAN = 80,
     PARAMENT_STATUS_INVALID_QUADRATURE_SELECTION = 90,
     PARAMENT_FAIL = 1000,
-    PARAMENT_STATUS_KERNEL_TIMEOUT = 1010, /* a bounded device-side wait gave up (batched queue) */
+    PARAMENT_STATUS_KERNEL_TIMEOUT = 1010, /* a bounded device-side wait of a tensor-core kernel gave up */
     PARAMENT_STATUS_SCRATCH_EXCEEDED = 1020 /* problem larger than Parament_equipropNoAlloc_fp64's fixed scratch */
 } Parament_ErrorCode;
 
@@ -120,13 +120,20 @@ PARAMENT_API void device_info(void);
  *   PARAMENT_PRECISION_PLAIN : the reference scheme in the context's own precision
  *                              (default; complex128 or complex64 arithmetic).
  *   PARAMENT_PRECISION_SPLIT : complex64 contexts only.  Step exponentials are
- *                              formed as U_j = I + E_j with the terms of first and
- *                              second order in the Hamiltonian in double-float
- *                              arithmetic and the higher orders in FP32; the
- *                              running product is accumulated in double-float and
- *                              the top of the product tree in FP64.  The Chebyshev
- *                              order is the smallest odd order whose truncation
- *                              summed over all steps stays below 1e-9. */
+ *                              formed as U_j = I + E_j from the same
+ *                              Chebyshev-Bessel polynomial regrouped by powers
+ *                              of X_j: the step's Hamiltonian X_j and the
+ *                              first-order term in double-float (pairs of
+ *                              floats), the higher powers as sliced products
+ *                              (bf16 slices of integers, accumulated exactly on
+ *                              the tensor cores) at d = 64 or FP32 products at
+ *                              d < 64; each chunk of consecutive steps is
+ *                              multiplied into a double-float running product
+ *                              (sliced products again at d = 64) and the chunk
+ *                              products are combined by a double-float tree.
+ *                              The Chebyshev order is the smallest odd order
+ *                              whose truncation summed over all steps stays
+ *                              below 1e-9. */
 typedef enum Parament_PrecisionMode {
     PARAMENT_PRECISION_PLAIN = 0,
     PARAMENT_PRECISION_SPLIT = 1
@@ -213,12 +220,28 @@ PARAMENT_API Parament_ErrorCode Parament_ensembleDestroy(Parament_Ensemble *ens)
  * returns without waiting.  Scratch lives in a fixed 24 MiB device array inside
  * the library (held on each GPU that loads it until exit).  Limits: complex128
  * contexts with dim <= 64; larger problems return
- * PARAMENT_STATUS_SCRATCH_EXCEEDED.  The first call on a device looks up the
+ * PARAMENT_STATUS_SCRATCH_EXCEEDED.  The first call on a device (and the first
+ * after a cudaDeviceReset, which gives the device a new context) looks up the
  * array's address (cudaGetSymbolAddress) -- make it before any stream capture.
  * All calls share the array: calls that overlap on the GPU race; serialise them. */
 PARAMENT_API Parament_ErrorCode Parament_equipropNoAlloc_fp64(Parament_Context_f64 *handle, const void *d_carr,
                                                               double dt, unsigned int pts, unsigned int amps,
                                                               void *d_out, void *stream);
+
+/* Completion and faults (new).  The device-buffer entry points queue their
+ * work and return.  Parament_synchronize waits until the last call's work on
+ * the context is done and returns PARAMENT_STATUS_KERNEL_TIMEOUT if a bounded
+ * device-side wait of one of its tensor-core kernels gave up since the last
+ * report (that call's result is then not valid), PARAMENT_STATUS_SUCCESS
+ * otherwise.  Such a give-up is also reported by the host-buffer entry point
+ * that ran the kernel, and by the next device-buffer call on the context once
+ * it is known (that call then queues nothing). */
+PARAMENT_API Parament_ErrorCode Parament_synchronize(Parament_Context_f32 *handle);
+PARAMENT_API Parament_ErrorCode Parament_synchronize_fp64(Parament_Context_f64 *handle);
+/* Bytes of device memory the context's buffers hold (Hamiltonian and work
+ * buffers; grow-only until Parament_destroy). */
+PARAMENT_API unsigned long long Parament_deviceMemoryBytes(Parament_Context_f32 *handle);
+PARAMENT_API unsigned long long Parament_deviceMemoryBytes_fp64(Parament_Context_f64 *handle);
 
 /* Instrumentation (new).  With timing enabled, each equiprop records CUDA
  * events on its stream around its dominant kernel (the fused step kernel, or

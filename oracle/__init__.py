@@ -173,9 +173,10 @@ def tree_product(mats, nthreads: int = 1) -> np.ndarray:
     return m[0]
 
 
-def scipy_expm_product(H0, H1, carr, dt, magnus=False, mode=NONE):
+def scipy_expm_product(H0, H1, carr, dt, magnus=False, mode=NONE, s0=0, s1=None):
     """Independent cross-check: scipy.linalg.expm of every step, multiplied in
-    time order (later step on the left), with the same expansion stack."""
+    time order (later step on the left), with the same expansion stack.  With
+    s0, s1 only the steps [s0, s1) are propagated (their ordered product)."""
     import scipy.linalg
 
     H0 = _c128(H0)
@@ -186,9 +187,56 @@ def scipy_expm_product(H0, H1, carr, dt, magnus=False, mode=NONE):
     h = 2.0 * dt if (magnus or mode == SIMPSON) else dt
     stack = build_stack(H0, H1, magnus)
     P = num_steps(mode, magnus, carr.shape[1])
+    s1 = P if s1 is None else min(s1, P)
     U = np.eye(d, dtype=np.complex128)
-    for s in range(P):
+    for s in range(s0, s1):
         w = step_weights(carr, K, mode, magnus, h, s)
         X = stack[0] + np.tensordot(w, stack[1:], axes=1)
         U = scipy.linalg.expm(-1j * h * X) @ U
     return U
+
+
+def _scipy_chunk(args):
+    """Worker of scipy_baseline: (seconds, product) of the steps [s0, s1)."""
+    import time
+    H0, H1, carr, dt, magnus, mode, s0, s1 = args
+    t0 = time.perf_counter()
+    U = scipy_expm_product(H0, H1, carr, dt, magnus, mode, s0, s1)
+    return time.perf_counter() - t0, U
+
+
+def scipy_baseline(H0, H1, carr, dt, magnus=False, mode=NONE, steps=None, procs=1):
+    """The NumPy/SciPy FP64 expm-product of the scheme timed on the host: the
+    first `steps` steps split into `procs` contiguous chunks, one process each
+    (spawned, with one BLAS/OpenMP thread per process), then the ordered
+    product of the chunk products.  Returns (steps/s, steps, wall seconds)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import time
+
+    carr = _c128(np.atleast_2d(carr))
+    P = num_steps(mode, magnus, carr.shape[1])
+    S = P if steps is None else min(P, int(steps))
+    bounds = [S * i // procs for i in range(procs + 1)]
+    jobs = [(H0, H1, carr, dt, magnus, mode, bounds[i], bounds[i + 1]) for i in range(procs)]
+    keep = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+    for k in keep:
+        os.environ[k] = "1"
+    try:
+        # A worker that fails to start breaks the executor (an exception here),
+        # where a multiprocessing.Pool would restart it forever.
+        with cf.ProcessPoolExecutor(procs, mp_context=mp.get_context("spawn")) as pool:
+            list(pool.map(_scipy_chunk, [(H0, H1, carr, dt, magnus, mode, 0, 1)] * procs))  # start-up, imports
+            t0 = time.perf_counter()
+            parts = list(pool.map(_scipy_chunk, jobs))
+            U = np.eye(np.shape(H0)[0], dtype=np.complex128)
+            for _, Ui in parts:
+                U = Ui @ U
+            wall = time.perf_counter() - t0
+    finally:
+        for k, v in keep.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    return S / wall, S, wall

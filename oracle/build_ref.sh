@@ -6,9 +6,14 @@
 #
 # deviceInfo.c is left out: it reads cudaDeviceProp::memoryClockRate, a field
 # that CUDA 13 removed, and it is not on the equiprop path.  No source is
-# edited.  Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
+# edited.  Usage: oracle/build_ref.sh <reference-root>, or with the root in
+# $PARAMENT_REFERENCE_ROOT.
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${PARAMENT_REFERENCE_ROOT:-}}
+if [ -z "$REF" ]; then
+    echo "usage: $0 <reference-root> (or set PARAMENT_REFERENCE_ROOT)" >&2
+    exit 2
+fi
 SRC="$REF/src/cuda"
 OUT="$(cd "$(dirname "$0")" && pwd)/_ref"
 if [ ! -f "$SRC/parament.cpp" ]; then

@@ -56,7 +56,27 @@ struct Ctx {
     // Work buffers (grow-only, like src/cuda/parament.cpp:418-474)
     DevBuf carr, out, chunks, work, X, B1, B2, aux, grad, wts, xplanes;
 
+    // Bounded-wait faults of this context's tensor-core kernels.  The kernels
+    // add to a device counter (d_fault, zero at creation, never reset); after
+    // each call that may run such a kernel the counter is copied into pinned
+    // host memory (h_fault) on the call's stream and ev_fault is recorded
+    // there.  A count above faults_seen is reported as
+    // PARAMENT_STATUS_KERNEL_TIMEOUT by the call itself (host-buffer entry
+    // points), by Parament_synchronize, or by the next device-buffer call on
+    // the context.
+    int *d_fault = nullptr;
+    int *h_fault = nullptr;
+    int faults_seen = 0;
+    cudaEvent_t ev_fault = nullptr;  // h_fault refreshed
+    bool fault_recorded = false;
+    cudaEvent_t ev_done = nullptr;   // end of the last call's work
+    bool done_recorded = false;
+
     size_t esize() const { return fp64 ? 16 : 8; }
+    size_t device_bytes() const {
+        return stack.cap + split_stack.cap + carr.cap + out.cap + chunks.cap + work.cap + X.cap + B1.cap + B2.cap +
+               aux.cap + grad.cap + wts.cap + xplanes.cap;
+    }
     void release_all() {
         stack.release();
         split_stack.release();
@@ -73,6 +93,13 @@ struct Ctx {
         xplanes.release();
     }
 };
+
+// Marks the end of a call's work on `stream`; with tensor_kernels set, the
+// fault counter is copied to the host there.  new_faults() reports whether a
+// kernel gave up since the last report (wait: block until the last call's
+// work is done; otherwise only look if it already is).
+void note_call_end(Ctx *c, cudaStream_t stream, bool tensor_kernels);
+bool new_faults(Ctx *c, bool wait);
 
 double onenorm_host(const void *m, unsigned d, bool fp64);
 int select_cycles(bool fp64, double hnorm, double dt);

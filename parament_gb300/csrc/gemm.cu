@@ -139,7 +139,7 @@ cudaError_t launch_gemm(const GemmLaunch &l) {
 }
 
 cudaError_t tree_product(bool fp64, int d, void *in, long long n, void *work, void *out, cudaStream_t stream,
-                         int num_sms, int *levels) {
+                         int num_sms, int *levels, int *fault) {
     if (levels) *levels = 0;
     const size_t es = fp64 ? 16 : 8;
     const long long dd = (long long)d * d;
@@ -167,6 +167,7 @@ cudaError_t tree_product(bool fp64, int d, void *in, long long n, void *work, vo
         g.alpha_re = 1.0;
         g.stream = stream;
         g.num_sms = num_sms;
+        g.fault = fault;
         cudaError_t e = launch_gemm(g);
         if (e != cudaSuccess) return e;
         if (levels) ++*levels;
@@ -267,6 +268,7 @@ static cudaError_t run_large(const LargeLaunch &l, int *launches) {
             g.diag_im = l.J[2 * k + 1];
             g.stream = l.stream;
             g.num_sms = l.num_sms;
+            g.fault = l.fault;
             e = launch_gemm(g);
             if (e != cudaSuccess) return e;
             if (launches) *launches += 1;
@@ -275,7 +277,7 @@ static cudaError_t run_large(const LargeLaunch &l, int *launches) {
         // b1 now holds the step exponentials of this batch.
         int lv = 0;
         e = tree_product(l.fp64, l.d, b1, cnt, b2, static_cast<char *>(l.out) + nb * dd * es, l.stream, l.num_sms,
-                         &lv);
+                         &lv, l.fault);
         if (e != cudaSuccess) return e;
         if (launches) *launches += lv;
     }

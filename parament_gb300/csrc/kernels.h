@@ -65,28 +65,26 @@ struct GemmLaunch {
     cudaStream_t stream;
     int num_sms;
     bool a_minus_identity;  // use A - I in place of A
+    int *fault;             // device counter of bounded waits that gave up (tensor-core kernel)
 };
 cudaError_t launch_gemm(const GemmLaunch &g);
 
 // tcgen05 tensor-core complex64 GEMM (3xTF32), used by launch_gemm for
-// complex64 with d >= 256 and d % 128 == 0.  tc_take_faults returns (and
-// clears) the number of CTAs whose bounded waits gave up.
+// complex64 with d >= 256 and d % 128 == 0.  A CTA whose bounded waits gave
+// up adds one to *g.fault (the calling context's device counter).
 bool tc_gemm_applies(const GemmLaunch &g);
 cudaError_t launch_tc_gemm(const GemmLaunch &g);
-int tc_take_faults();
 
 // Tensor-core form of the split complex64 kernel (d = 64): whether it serves
-// this problem, and the number (cleared on read) of CTAs whose bounded waits
-// on the tensor core gave up.
+// this problem.
 bool split_tc_applies(int d, int Ke, int M);
-int split_tc_take_faults();
 
 // Ordered product of n d x d matrices (later index on the left), pairwise tree
 // as src/cuda/parament.cpp:677-714.  `work` holds n*d*d elements and may be
 // overwritten; `in` is overwritten too.  The result is copied into `out`.
 // *levels (if given) receives the number of kernel launches.
 cudaError_t tree_product(bool fp64, int d, void *in, long long n, void *work, void *out, cudaStream_t stream,
-                         int num_sms, int *levels = nullptr);
+                         int num_sms, int *levels = nullptr, int *fault = nullptr);
 
 // Large-d plain path: the steps [s0, s1) are assembled, exponentiated and
 // multiplied into one product written to `out`.  Buffers: X, B1, B2 each hold
@@ -107,6 +105,7 @@ struct LargeLaunch {
     void *out;
     cudaStream_t stream;
     int num_sms;
+    int *fault;  // device fault counter of the context (tensor-core products)
 };
 cudaError_t launch_large_range(const LargeLaunch &a, int *launches = nullptr);
 

@@ -18,15 +18,20 @@
 //    many SMs that one chunk per resident CTA would not fit, fewer chunks are
 //    used (same result, less parallelism).
 //  - The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current).  Make
-//    that first call before any stream capture.
+//    cudaGetSymbolAddress (once per device and CUDA context, with that device
+//    current).  Make that first call before any stream capture.  After a
+//    cudaDeviceReset the device gets a new context and the library image is
+//    loaded again, possibly at another address: the next call sees the new
+//    context and looks the address up again (make it outside capture too).
 //  - All calls share the one array and it keeps the previous call's contents.
 //    Nothing here reads a scratch element before writing it, so nothing needs
 //    clearing -- but two calls whose work overlaps on the GPU (different
 //    streams, different contexts, different host threads) race on the array.
 //    Serialise them.
+#include <cuda.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <mutex>
@@ -44,22 +49,57 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 static std::mutex g_noalloc_mu;
 static void *g_noalloc_ptr[kNoAllocMaxDevices];
+static CUcontext g_noalloc_ctx[kNoAllocMaxDevices];
+
+// The calling thread's current CUDA context (the driver's cuCtxGetCurrent,
+// reached through the runtime's entry-point query so that no link against the
+// driver library is needed); null if unavailable.
+static CUcontext current_context() {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    static GetCurrent fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<GetCurrent>(p);
+    }();
+    CUcontext ctx = nullptr;
+    if (!fn || fn(&ctx) != CUDA_SUCCESS) return nullptr;
+    return ctx;
+}
 
 // Device address of the scratch array on `device` (which must be current).
+// Looked up once per device and context: a reset device has a new context.
 static cudaError_t noalloc_scratch(int device, void **out) {
     if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    const CUcontext ctx = current_context();
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
+    if (!g_noalloc_ptr[device] || !ctx || g_noalloc_ctx[device] != ctx) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             cudaGetLastError();
+            g_noalloc_ptr[device] = nullptr;
             return e != cudaSuccess ? e : cudaErrorInvalidSymbol;
         }
         g_noalloc_ptr[device] = p;
+        g_noalloc_ctx[device] = ctx;
     }
     *out = g_noalloc_ptr[device];
     return cudaSuccess;
+}
+
+// Usable scratch bytes: the whole array, or less when the environment variable
+// PARAMENT_NOALLOC_SCRATCH_BYTES asks for less (read once; a test hook that
+// forces the reduced chunk count a GPU with very many SMs would get).
+static size_t usable_scratch_bytes() {
+    static const size_t n = [] {
+        const char *v = getenv("PARAMENT_NOALLOC_SCRATCH_BYTES");
+        const long long b = v ? atoll(v) : 0;
+        return (b > 0 && (size_t)b < kNoAllocScratchBytes) ? (size_t)b : kNoAllocScratchBytes;
+    }();
+    return n;
 }
 
 }  // namespace pgb
@@ -77,15 +117,18 @@ extern "C" Parament_ErrorCode Parament_equipropNoAlloc_fp64(Parament_Context_f64
         return c->last_error = PARAMENT_FAIL;
     }
     cudaStream_t stream = stream_p ? static_cast<cudaStream_t>(stream_p) : c->stream;
+    // Argument checks in the order of the regular device entry point, then the
+    // size limit of the scratch array.
     if (!c->has_h) return c->last_error = PARAMENT_STATUS_NO_HAMILTONIAN;
-    if (amps > c->K || (amps > 0 && !d_carr)) return c->last_error = PARAMENT_STATUS_INVALID_VALUE;
-    const int d = (int)c->dim;
-    if (d > kSmallMaxDim) return c->last_error = PARAMENT_STATUS_SCRATCH_EXCEEDED;
+    if (amps > c->K) return c->last_error = PARAMENT_STATUS_INVALID_VALUE;
     const double h = (c->magnus || c->quad == PARAMENT_QUADRATURE_SIMPSON) ? 2.0 * dt : dt;
     const long long P = num_steps(c->quad, c->magnus, pts);
     if (P <= 0 || !(dt >= 0.0) || !isfinite(dt)) return c->last_error = PARAMENT_STATUS_INVALID_VALUE;
+    if (amps > 0 && !d_carr) return c->last_error = PARAMENT_STATUS_INVALID_VALUE;
     int M = c->manual ? (int)c->mmax : select_cycles(true, c->hnorm, h);
     if (M < 3 && !c->manual) return c->last_error = PARAMENT_STATUS_SELECT_SMALLER_DT;
+    const int d = (int)c->dim;
+    if (d > kSmallMaxDim) return c->last_error = PARAMENT_STATUS_SCRATCH_EXCEEDED;
     void *scratch = nullptr;
     if (noalloc_scratch(c->device, &scratch) != cudaSuccess) return c->last_error = PARAMENT_FAIL;
     if (c->hnorm == 0.0 || dt == 0.0) {
@@ -94,11 +137,12 @@ extern "C" Parament_ErrorCode Parament_equipropNoAlloc_fp64(Parament_Context_f64
             return c->last_error = PARAMENT_STATUS_CUBLAS_FAILED;
         }
         c->last_M = M;
+        c->launches = 1;
         return c->last_error = PARAMENT_STATUS_SUCCESS;
     }
     // Chunk products and the tree's second buffer: 2 * nchunks * d^2 complex128.
     const size_t per_chunk = 2 * sizeof(double) * 2 * (size_t)d * d;
-    const long long fit = (long long)(kNoAllocScratchBytes / per_chunk);
+    const long long fit = (long long)(usable_scratch_bytes() / per_chunk);
     const int nch = (int)std::min<long long>(small_chunk_count(true, d, (int)c->Ke, P, c->num_sms), fit);
     if (nch < 1) return c->last_error = PARAMENT_STATUS_SCRATCH_EXCEEDED;
     char *chunks = static_cast<char *>(scratch);
@@ -119,8 +163,12 @@ extern "C" Parament_ErrorCode Parament_equipropNoAlloc_fp64(Parament_Context_f64
     l.P = P;
     l.nchunks = nch;
     l.stream = stream;
+    if (c->timing) cudaEventRecord(c->ev_start, stream);
     cudaError_t e = launch_small_steps(l);
-    if (e == cudaSuccess) e = tree_product(true, d, chunks, nch, work, d_out, stream, c->num_sms);
+    if (c->timing) cudaEventRecord(c->ev_stop, stream);
+    int levels = 0;
+    if (e == cudaSuccess) e = tree_product(true, d, chunks, nch, work, d_out, stream, c->num_sms, &levels);
+    c->launches = 1 + levels;
     if (e != cudaSuccess) {
         cudaGetLastError();
         return c->last_error = PARAMENT_STATUS_CUBLAS_FAILED;

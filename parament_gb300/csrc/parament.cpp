@@ -113,6 +113,28 @@ long long num_steps(int quad, bool magnus, unsigned pts) {
     return pts;
 }
 
+void note_call_end(Ctx *c, cudaStream_t stream, bool tensor_kernels) {
+    if (tensor_kernels &&
+        cudaMemcpyAsync(c->h_fault, c->d_fault, sizeof(int), cudaMemcpyDeviceToHost, stream) == cudaSuccess &&
+        cudaEventRecord(c->ev_fault, stream) == cudaSuccess)
+        c->fault_recorded = true;
+    if (cudaEventRecord(c->ev_done, stream) == cudaSuccess) c->done_recorded = true;
+    cudaGetLastError();
+}
+
+bool new_faults(Ctx *c, bool wait) {
+    if (!c->fault_recorded) return false;
+    cudaError_t e = wait ? cudaEventSynchronize(c->ev_fault) : cudaEventQuery(c->ev_fault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const int v = *static_cast<volatile int *>(c->h_fault);
+    if (v <= c->faults_seen) return false;
+    c->faults_seen = v;
+    return true;
+}
+
 }  // namespace pgb
 
 // ------------------------------------------------------------------ life cycle
@@ -131,6 +153,25 @@ static Parament_ErrorCode ctx_create(Ctx **out, bool fp64) {
         *out = nullptr;
         return PARAMENT_STATUS_CUBLAS_INIT_FAILED;
     }
+    // The fault counter and its host mirror (set-up allocations, not counted by
+    // the allocation-failure injection of the work buffers).
+    if (cudaMalloc(&c->d_fault, sizeof(int)) != cudaSuccess ||
+        cudaHostAlloc(&c->h_fault, sizeof(int), cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fault, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMemsetAsync(c->d_fault, 0, sizeof(int), c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        if (c->d_fault) cudaFree(c->d_fault);
+        if (c->h_fault) cudaFreeHost(c->h_fault);
+        if (c->ev_done) cudaEventDestroy(c->ev_done);
+        if (c->ev_fault) cudaEventDestroy(c->ev_fault);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        *out = nullptr;
+        return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+    }
+    *c->h_fault = 0;
     c->last_error = PARAMENT_STATUS_SUCCESS;
     return PARAMENT_STATUS_SUCCESS;
 }
@@ -139,9 +180,15 @@ static Parament_ErrorCode ctx_destroy(Ctx *c) {
     if (!c) return PARAMENT_STATUS_SUCCESS;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    if (c->done_recorded) cudaEventSynchronize(c->ev_done);
+    if (c->fault_recorded) cudaEventSynchronize(c->ev_fault);
     c->release_all();
     if (c->ev_start) cudaEventDestroy(c->ev_start);
     if (c->ev_stop) cudaEventDestroy(c->ev_stop);
+    cudaEventDestroy(c->ev_done);
+    cudaEventDestroy(c->ev_fault);
+    cudaFree(c->d_fault);
+    cudaFreeHost(c->h_fault);
     cudaStreamDestroy(c->stream);
     delete c;
     return PARAMENT_STATUS_SUCCESS;
@@ -195,6 +242,7 @@ static Parament_ErrorCode set_hamiltonian(Ctx *c, const void *H0, const void *H1
         g.alpha_re = 1.0;
         g.stream = c->stream;
         g.num_sms = c->num_sms;
+        g.fault = c->d_fault;
         cudaError_t r = launch_gemm(g);
         if (r != cudaSuccess) return r;
         g.A = st + es * dd * b;
@@ -210,11 +258,16 @@ static Parament_ErrorCode set_hamiltonian(Ctx *c, const void *H0, const void *H1
             for (unsigned j = 0; j < i && e == cudaSuccess; ++j)
                 e = commutator(1 + j, 1 + i, 1 + 2 * amps + i * (i - 1) / 2 + j);
     }
+    if (use_magnus) note_call_end(c, c->stream, true);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         c->stack.release();
         return c->last_error = PARAMENT_STATUS_CUBLAS_FAILED;
+    }
+    if (new_faults(c, true)) {
+        c->stack.release();
+        return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
     }
     c->dim = dim;
     c->K = amps;
@@ -261,7 +314,8 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
         if (c->timing) cudaEventRecord(c->ev_stop, stream);
         int levels = 0;
         if (e == cudaSuccess)
-            e = tree_product(c->fp64, d, c->chunks.ptr, nch, c->work.ptr, d_out, stream, c->num_sms, &levels);
+            e = tree_product(c->fp64, d, c->chunks.ptr, nch, c->work.ptr, d_out, stream, c->num_sms, &levels,
+                             c->d_fault);
         c->launches = 1 + levels;
     } else {
         // Batches of G steps held as X, b_(k+1), b_(k+2): 3 G d^2 elements, capped near 4 GiB.
@@ -292,13 +346,15 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
         l.out = c->chunks.ptr;
         l.stream = stream;
         l.num_sms = c->num_sms;
+        l.fault = c->d_fault;
         if (c->timing) cudaEventRecord(c->ev_start, stream);
         int launched = 0;
         e = launch_large_range(l, &launched);
         if (c->timing) cudaEventRecord(c->ev_stop, stream);
         int levels = 0;
         if (e == cudaSuccess)
-            e = tree_product(c->fp64, d, c->chunks.ptr, nb, c->work.ptr, d_out, stream, c->num_sms, &levels);
+            e = tree_product(c->fp64, d, c->chunks.ptr, nb, c->work.ptr, d_out, stream, c->num_sms, &levels,
+                             c->d_fault);
         c->launches = launched + levels;
     }
     if (e != cudaSuccess) {
@@ -306,6 +362,13 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
         return PARAMENT_STATUS_CUBLAS_FAILED;
     }
     return PARAMENT_STATUS_SUCCESS;
+}
+
+// Whether an equiprop of this context may launch a kernel with bounded waits
+// (the tensor-core GEMM of complex64 contexts with d > 64, the tensor-core
+// split kernel).
+static bool uses_tensor_kernels(const Ctx *c) {
+    return !c->fp64 && (c->dim > (unsigned)kSmallMaxDim || c->precision == PARAMENT_PRECISION_SPLIT);
 }
 
 // Checks, order selection and dispatch shared by the host and device entry
@@ -361,6 +424,7 @@ static Parament_ErrorCode equiprop_host(Ctx *c, const void *carr, double dt, uns
         cudaStreamSynchronize(c->stream);
         return c->last_error = r;
     }
+    note_call_end(c, c->stream, uses_tensor_kernels(c));
     // Result back to the host (src/cuda/parament.cpp:846).
     cudaError_t e = cudaMemcpyAsync(out, c->out.ptr, es * dd, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -368,15 +432,24 @@ static Parament_ErrorCode equiprop_host(Ctx *c, const void *carr, double dt, uns
         cudaGetLastError();
         return c->last_error = PARAMENT_STATUS_CUBLAS_FAILED;
     }
-    if (!c->fp64 && c->dim > (unsigned)kSmallMaxDim && tc_take_faults() > 0)
-        return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
-    if (!c->fp64 && c->precision == PARAMENT_PRECISION_SPLIT && split_tc_applies((int)c->dim, (int)c->Ke, c->last_M) &&
-        split_tc_take_faults() > 0)
-        return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
+    if (new_faults(c, true)) return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
     return c->last_error = PARAMENT_STATUS_SUCCESS;
 }
 
 static Ctx *as_ctx(void *p) { return static_cast<Ctx *>(p); }
+
+// Device-buffer entry points: the work is queued and not waited for.  A
+// bounded wait that gave up in an earlier call of the context is reported
+// here, once it is known, before anything new is queued.
+static Parament_ErrorCode equiprop_device_call(Ctx *c, const void *d_carr, double dt, unsigned pts, unsigned amps,
+                                               void *d_out, void *stream_p) {
+    cudaSetDevice(c->device);
+    if (new_faults(c, false)) return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
+    cudaStream_t stream = stream_p ? static_cast<cudaStream_t>(stream_p) : c->stream;
+    Parament_ErrorCode r = equiprop_device(c, d_carr, dt, pts, amps, d_out, stream);
+    if (r == PARAMENT_STATUS_SUCCESS) note_call_end(c, stream, uses_tensor_kernels(c));
+    return c->last_error = r;
+}
 
 // ------------------------------------------------------------ exported C-ABI
 
@@ -540,19 +613,13 @@ double Parament_hamiltonianNorm_fp64(Parament_Context_f64 *handle) {
 Parament_ErrorCode Parament_equipropDevice(Parament_Context_f32 *handle, const void *d_carr, double dt,
                                            unsigned int pts, unsigned int amps, void *d_out, void *stream) {
     if (!handle || !d_out) return PARAMENT_STATUS_INVALID_VALUE;
-    Ctx *c = as_ctx(handle);
-    cudaSetDevice(c->device);
-    return c->last_error = equiprop_device(c, d_carr, dt, pts, amps, d_out,
-                                           stream ? static_cast<cudaStream_t>(stream) : c->stream);
+    return equiprop_device_call(as_ctx(handle), d_carr, dt, pts, amps, d_out, stream);
 }
 
 Parament_ErrorCode Parament_equipropDevice_fp64(Parament_Context_f64 *handle, const void *d_carr, double dt,
                                                 unsigned int pts, unsigned int amps, void *d_out, void *stream) {
     if (!handle || !d_out) return PARAMENT_STATUS_INVALID_VALUE;
-    Ctx *c = as_ctx(handle);
-    cudaSetDevice(c->device);
-    return c->last_error = equiprop_device(c, d_carr, dt, pts, amps, d_out,
-                                           stream ? static_cast<cudaStream_t>(stream) : c->stream);
+    return equiprop_device_call(as_ctx(handle), d_carr, dt, pts, amps, d_out, stream);
 }
 
 static Parament_ErrorCode vjp_host(Ctx *c, const void *carr, double dt, unsigned pts, unsigned amps, const void *W,
@@ -586,6 +653,16 @@ static Parament_ErrorCode vjp_host(Ctx *c, const void *carr, double dt, unsigned
     return c->last_error = PARAMENT_STATUS_SUCCESS;
 }
 
+static Parament_ErrorCode vjp_device_call(Ctx *c, const void *d_carr, double dt, unsigned pts, unsigned amps,
+                                          const void *d_W, void *d_grad, void *stream_p) {
+    cudaSetDevice(c->device);
+    if (new_faults(c, false)) return c->last_error = PARAMENT_STATUS_KERNEL_TIMEOUT;
+    cudaStream_t stream = stream_p ? static_cast<cudaStream_t>(stream_p) : c->stream;
+    Parament_ErrorCode r = run_vjp(c, d_carr, dt, pts, amps, d_W, d_grad, stream);
+    if (r == PARAMENT_STATUS_SUCCESS) note_call_end(c, stream, false);
+    return c->last_error = r;
+}
+
 Parament_ErrorCode Parament_equipropVJP(Parament_Context_f32 *handle, cuComplex *carr, double dt, unsigned int pts,
                                         unsigned int amps, cuComplex *W, float *grad) {
     if (!handle) return PARAMENT_STATUS_INVALID_VALUE;
@@ -600,19 +677,13 @@ Parament_ErrorCode Parament_equipropVJPDevice(Parament_Context_f32 *handle, cons
                                               unsigned int pts, unsigned int amps, const void *d_W, void *d_grad,
                                               void *stream) {
     if (!handle) return PARAMENT_STATUS_INVALID_VALUE;
-    Ctx *c = as_ctx(handle);
-    cudaSetDevice(c->device);
-    return c->last_error = run_vjp(c, d_carr, dt, pts, amps, d_W, d_grad,
-                                   stream ? static_cast<cudaStream_t>(stream) : c->stream);
+    return vjp_device_call(as_ctx(handle), d_carr, dt, pts, amps, d_W, d_grad, stream);
 }
 Parament_ErrorCode Parament_equipropVJPDevice_fp64(Parament_Context_f64 *handle, const void *d_carr, double dt,
                                                    unsigned int pts, unsigned int amps, const void *d_W, void *d_grad,
                                                    void *stream) {
     if (!handle) return PARAMENT_STATUS_INVALID_VALUE;
-    Ctx *c = as_ctx(handle);
-    cudaSetDevice(c->device);
-    return c->last_error = run_vjp(c, d_carr, dt, pts, amps, d_W, d_grad,
-                                   stream ? static_cast<cudaStream_t>(stream) : c->stream);
+    return vjp_device_call(as_ctx(handle), d_carr, dt, pts, amps, d_W, d_grad, stream);
 }
 
 static Parament_ErrorCode set_timing(Ctx *c, int enable) {
@@ -645,6 +716,31 @@ Parament_ErrorCode Parament_setKernelTiming_fp64(Parament_Context_f64 *handle, i
 }
 float Parament_lastKernelMs(Parament_Context_f32 *handle) { return handle ? kernel_ms(as_ctx(handle)) : -1.0f; }
 float Parament_lastKernelMs_fp64(Parament_Context_f64 *handle) { return handle ? kernel_ms(as_ctx(handle)) : -1.0f; }
+static Parament_ErrorCode ctx_synchronize(Ctx *c) {
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaSuccess;
+    if (c->done_recorded) e = cudaEventSynchronize(c->ev_done);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return c->last_error = PARAMENT_FAIL;
+    }
+    return c->last_error = new_faults(c, true) ? PARAMENT_STATUS_KERNEL_TIMEOUT : PARAMENT_STATUS_SUCCESS;
+}
+
+Parament_ErrorCode Parament_synchronize(Parament_Context_f32 *handle) {
+    return handle ? ctx_synchronize(as_ctx(handle)) : PARAMENT_STATUS_INVALID_VALUE;
+}
+Parament_ErrorCode Parament_synchronize_fp64(Parament_Context_f64 *handle) {
+    return handle ? ctx_synchronize(as_ctx(handle)) : PARAMENT_STATUS_INVALID_VALUE;
+}
+unsigned long long Parament_deviceMemoryBytes(Parament_Context_f32 *handle) {
+    return handle ? (unsigned long long)as_ctx(handle)->device_bytes() : 0ULL;
+}
+unsigned long long Parament_deviceMemoryBytes_fp64(Parament_Context_f64 *handle) {
+    return handle ? (unsigned long long)as_ctx(handle)->device_bytes() : 0ULL;
+}
+
 int Parament_lastLaunchCount(Parament_Context_f32 *handle) { return handle ? as_ctx(handle)->launches : 0; }
 int Parament_lastLaunchCount_fp64(Parament_Context_f64 *handle) { return handle ? as_ctx(handle)->launches : 0; }
 

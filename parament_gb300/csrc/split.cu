@@ -548,6 +548,7 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
     a.mode = c->quad;
     a.magnus = c->magnus ? 1 : 0;
     a.hfac = h / 12.0;
+    a.fault = c->d_fault;
     const size_t dd = (size_t)d * d;
     const bool tensor = split_tc_applies(d, (int)c->Ke, M);
     const void *fn = pick_split(d);

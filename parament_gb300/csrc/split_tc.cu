@@ -40,7 +40,8 @@
 // work (slicing, epilogues) that surrounds each product; each thread owns one
 // plane of 16 columns of one row.  While the tensor core runs X Q, the threads
 // slice E^P, the B operand of the running product.  Every wait on the tensor core is bounded: a wait that
-// runs out stops the CTA, counts a fault and frees tensor memory.
+// runs out stops the CTA, adds one to the calling context's fault counter and
+// frees tensor memory.
 #include <math.h>
 #include <stdlib.h>
 
@@ -81,6 +82,7 @@ constexpr uint32_t kTcdXBytes = 4 * kTcdPlane * sizeof(float);
 static_assert(kTcdXBytes <= kTcdSA && kTcdXBytes % 16 == 0, "planes exceed the A slice buffer");
 static_assert(kTcdPlane * 4 == kSplitXStride, "plane layout of k_split_assemble");
 
+// Bounded waits that gave up, for launches without a context's counter.
 __device__ int g_split_tc_faults;
 
 // Bulk copy global -> shared memory completing on an mbarrier (transaction
@@ -616,7 +618,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         }
     }
     if (!ok) {
-        if (t.tid == 0) atomicAdd(&g_split_tc_faults, 1);
+        if (t.tid == 0) atomicAdd(a.fault ? a.fault : &g_split_tc_faults, 1);
         // Let any product or copy still in flight finish before tensor memory
         // and shared memory are released.
         if (ncommit > 0) tc::mbar_wait(&sh.bar, (ncommit - 1) & 1, kTcdWait);
@@ -801,19 +803,6 @@ cudaError_t launch_split_tc(const SplitArgs &a, int num_sms, float *xplanes, int
     if (ev1) cudaEventRecord(ev1, stream);
     *nchunks = total;
     return cudaSuccess;
-}
-
-int split_tc_take_faults() {
-    int v = 0;
-    if (cudaMemcpyFromSymbol(&v, g_split_tc_faults, sizeof(int)) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    if (v) {
-        int z = 0;
-        cudaMemcpyToSymbol(g_split_tc_faults, &z, sizeof(int));
-    }
-    return v;
 }
 
 }  // namespace pgb

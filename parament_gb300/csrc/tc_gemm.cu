@@ -73,7 +73,8 @@ __device__ __forceinline__ void tc_tma_load3(void *dst, const CUtensorMap *map, 
         : "memory");
 }
 
-__device__ int g_tc_faults;  // bounded waits that gave up (0 in normal operation)
+// Bounded waits that gave up, for launches without a context's counter.
+__device__ int g_tc_faults;
 
 struct TcArgs {
     // A and B as 3-D FP32 tensors (2 d floats per row, d rows, batch items);
@@ -86,6 +87,7 @@ struct TcArgs {
     float2 alpha, diag;
     float beta;
     int d, batch, tiles_n, a_minus_identity;
+    int *fault;  // the calling context's counter of CTAs whose waits gave up
 };
 
 __device__ __forceinline__ float4 lds128(uint32_t a) {
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
             }
         }
     }
-    if (!ok) atomicAdd(&g_tc_faults, 1);
+    if (!ok) atomicAdd(g.fault ? g.fault : &g_tc_faults, 1);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == kTcIssuer) {
@@ -411,6 +413,7 @@ cudaError_t launch_tc_gemm(const GemmLaunch &l) {
     g.batch = l.batch;
     g.tiles_n = l.d / 128;
     g.a_minus_identity = l.a_minus_identity ? 1 : 0;
+    g.fault = l.fault;
     if (!make_map(&g.tmA, l.A, l.d, l.strideA, l.batch, 32, 128, CU_TENSOR_MAP_SWIZZLE_128B, &g.batchedA) ||
         !make_map(&g.tmB, l.B, l.d, l.strideB, l.batch, 256, 16, CU_TENSOR_MAP_SWIZZLE_NONE, &g.batchedB))
         return cudaErrorInvalidValue;
@@ -424,19 +427,6 @@ cudaError_t launch_tc_gemm(const GemmLaunch &l) {
     const int grid = (int)std::min<long long>(units, sms);
     k_tc_cgemm<<<grid, kTcThreads, smem, l.stream>>>(g);
     return cudaGetLastError();
-}
-
-int tc_take_faults() {
-    int v = 0;
-    if (cudaMemcpyFromSymbol(&v, g_tc_faults, sizeof(int)) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    if (v) {
-        int z = 0;
-        cudaMemcpyToSymbol(g_tc_faults, &z, sizeof(int));
-    }
-    return v;
 }
 
 }  // namespace pgb

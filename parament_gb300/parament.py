@@ -227,7 +227,10 @@ class Parament:
     @_must_be_alive
     def set_precision_mode(self, mode):
         """'plain' (the reference scheme, default) or 'split' (complex64 contexts:
-        double-float first/second-order terms, FP64 top of the product tree)."""
+        U_j = I + E_j with X_j and the first-order term in double-float, the
+        higher powers as sliced bf16 products with exact accumulation on the
+        tensor cores at d = 64 (FP32 products below), a double-float running
+        product per chunk of steps and a double-float tree of the chunks)."""
         if self._use_doubles and mode != 'plain':
             raise ValueError("the split precision form applies to 'fp32' contexts only")
         code = {'plain': PARAMENT_PRECISION_PLAIN, 'split': PARAMENT_PRECISION_SPLIT}.get(mode)
@@ -264,6 +267,19 @@ class Parament:
                                                    amps, ctypes.c_void_p(out.data_ptr()), _stream_handle(stream))
         self._check_error(code)
         return out
+
+    @_must_be_alive
+    def synchronize(self):
+        """Wait for the work queued by the device-buffer calls of this context;
+        raises RuntimeError (code 1010) if a bounded wait of a tensor-core
+        kernel gave up since the last report."""
+        self._check_error(self._fn('Parament_synchronize')(self._handle))
+
+    @property
+    @_must_be_alive
+    def device_memory_bytes(self):
+        """Bytes of device memory held by this context's buffers."""
+        return int(self._fn('Parament_deviceMemoryBytes')(self._handle))
 
     @_must_be_alive
     def vjp(self, dt, W, *carr):

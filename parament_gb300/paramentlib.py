@@ -84,6 +84,9 @@ for _name in ("Parament_equipropDevice", "Parament_equipropDevice_fp64"):
     getattr(lib, _name).argtypes = [c_ParamentContext_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_uint,
                                     ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p]
 for _sfx in ("", "_fp64"):
+    getattr(lib, "Parament_synchronize" + _sfx).argtypes = [c_ParamentContext_p]
+    getattr(lib, "Parament_deviceMemoryBytes" + _sfx).argtypes = [c_ParamentContext_p]
+    getattr(lib, "Parament_deviceMemoryBytes" + _sfx).restype = ctypes.c_ulonglong
     getattr(lib, "Parament_setKernelTiming" + _sfx).argtypes = [c_ParamentContext_p, ctypes.c_int]
     getattr(lib, "Parament_lastKernelMs" + _sfx).argtypes = [c_ParamentContext_p]
     getattr(lib, "Parament_lastKernelMs" + _sfx).restype = ctypes.c_float

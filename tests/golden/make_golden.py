@@ -131,6 +131,7 @@ def save_cases(cases):
 def ref_host_values():
     so = os.path.join(ROOT, "oracle", "_ref", "libparament_ref.so")
     if not os.path.exists(so):
+        # the reference root comes from $PARAMENT_REFERENCE_ROOT (build_ref.sh)
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
     L = ctypes.CDLL(so)
     for n in ("Parament_selectIterationCycles_fp32", "Parament_selectIterationCycles_fp64"):

@@ -179,6 +179,7 @@ def test_device_entry_point_matches_host(built_lib, precision):
         ct = torch.complex128 if precision == "fp64" else torch.complex64
         carr = torch.tensor(w["carr"], dtype=ct, device="cuda")
         Ud = ctx.equiprop_device(w["dt"], carr)
+        ctx.synchronize()  # no bounded wait gave up
         torch.cuda.synchronize()
         assert np.array_equal(Ud.cpu().numpy(), Uh)
 
