@@ -171,7 +171,11 @@ PARAMENT_API Parament_ErrorCode Parament_equipropDevice_fp64(Parament_Context_f6
  * Controls are taken as real: the imaginary parts of the samples enter U but
  * get no derivative.  grad is float for complex64 contexts and double for
  * complex128 ones.  Limits: dim <= 64 (complex64) or 48 (complex128).
- * Memory: one d x d checkpoint per step plus Ke traces per step. */
+ * Memory: Ke traces per step plus five d x d matrices per chunk of steps
+ * (about one chunk per resident CTA; the chunk boundaries are the
+ * checkpoints, the propagators between them are recomputed).  With a manual
+ * Chebyshev order the step exponentials need not be unitary, and one d x d
+ * matrix per step is stored instead. */
 PARAMENT_API Parament_ErrorCode Parament_equipropVJP(Parament_Context_f32 *handle, cuComplex *carr, double dt,
                                                      unsigned int pts, unsigned int amps, cuComplex *W, float *grad);
 PARAMENT_API Parament_ErrorCode Parament_equipropVJP_fp64(Parament_Context_f64 *handle, cuDoubleComplex *carr,

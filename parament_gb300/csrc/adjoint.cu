@@ -20,11 +20,21 @@
 // gradients through the quadrature weights.
 //
 // Schedule (one launch per phase):
-//   1. chunk products S_c of nc chunks of consecutive steps (k_small_steps);
-//   2. exclusive prefix/suffix products of the chunks (Hillis-Steele scans);
-//   3. one CTA per chunk: forward sweep from the chunk's prefix that stores
-//      the checkpoints R_j, then the backward sweep carrying M_j = W^H L_j,
-//      forming B_j = R_j M_j, U_j and Gamma_j together, and the traces t_m[j];
+//   1. chunk products S_c of nc chunks of consecutive steps (k_small_steps),
+//      nc about one per SM, so that the chunk boundaries -- the checkpoints --
+//      come every P / nc steps (about sqrt(P) steps at the gradient workload,
+//      16384 steps in 152 chunks);
+//   2. exclusive prefix/suffix products of the chunks (Hillis-Steele scans):
+//      R at every chunk start and L at every chunk end;
+//   3. one CTA per chunk sweeps its steps backward carrying M_j = W^H L_j and
+//      recomputing the rest: U_j from X_j, R_j = U_j^H R_(j+1) from the
+//      chunk-end checkpoint R_(s1) = S_c R_(s0) (the step exponentials of the
+//      automatic order are unitary to working precision), B_j = R_j M_j,
+//      then U_j and Gamma_j together, and the traces t_m[j].  Nothing per
+//      step is stored but the Ke traces.  A manual Chebyshev order can leave
+//      U_j far from unitary; then the CTA first sweeps forward from R_(s0)
+//      storing every R_j of its chunk (one d x d matrix per step) and the
+//      backward sweep reads them;
 //   4. sample gradients from the traces (quadrature / Magnus adjoint).
 #include <algorithm>
 #include <vector>
@@ -43,11 +53,13 @@ struct AdjArgs {
     const cplx_t<R> *pre;  // nc exclusive prefix products (R at each chunk start)
     const cplx_t<R> *suf;  // nc exclusive suffix products (L at each chunk end)
     const cplx_t<R> *W;    // seed, d x d
-    cplx_t<R> *Rbuf;       // P checkpoints R_j
+    const cplx_t<R> *chunks;  // nc chunk products S_c
+    cplx_t<R> *Rbuf;       // P stored R_j (stored form only)
     cplx_t<R> *tr;         // P x Ke traces
     long long P;
     int nchunks;
     int d, Ke, M;
+    int reversible;        // 1: R_j = U_j^H R_(j+1) in the backward sweep; 0: stored R_j
     R s;
     WeightSpec w;
 };
@@ -112,21 +124,10 @@ __global__ void __launch_bounds__(256) k_adj_chunks(const __grid_constant__ AdjA
             }
     };
 
-    // ---- forward sweep: checkpoints R_j for j in [s0, s1)
-#pragma unroll
-    for (int i = 0; i < TM; ++i)
-#pragma unroll
-        for (int j = 0; j < TM; ++j)
-            if (own[i][j]) Rs[eo[i][j]] = a.pre[(size_t)blockIdx.x * dd + ge[i][j]];
-    for (long long st = s0; st < s1; ++st) {
-#pragma unroll
-        for (int i = 0; i < TM; ++i)
-#pragma unroll
-            for (int j = 0; j < TM; ++j)
-                if (own[i][j]) a.Rbuf[(size_t)st * dd + ge[i][j]] = Rs[eo[i][j]];
-        if (st + 1 == s1) break;
-        assemble(st);
-        // U_st by the reference's Clenshaw recurrence (own elements in acc).
+    // U of the step in Xs by the reference's Clenshaw recurrence (own
+    // elements in acc; B1 is scratch).  Starts and ends with all threads past
+    // their last read of B1.
+    auto clenshaw_u = [&]() {
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -165,15 +166,17 @@ __global__ void __launch_bounds__(256) k_adj_chunks(const __grid_constant__ AdjA
                 }
             if (k > 0) __syncthreads();
         }
-        // R <- U R = R + (U - I) R
+    };
+
+    if (a.reversible) {
+        // ---- checkpoint at the chunk end: R_(s1) = S_c R_(s0)
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
             for (int j = 0; j < TM; ++j)
                 if (own[i][j]) {
-                    C u = acc[i][j];
-                    if (dg[i][j]) u.x -= (R)1;
-                    B1[eo[i][j]] = u;
+                    B1[eo[i][j]] = a.chunks[(size_t)blockIdx.x * dd + ge[i][j]];
+                    Rs[eo[i][j]] = a.pre[(size_t)blockIdx.x * dd + ge[i][j]];
                 }
         __syncthreads();
         tile_gemm<C, TM>(acc, B1, Rs, d, ld, ty, tx);
@@ -182,8 +185,43 @@ __global__ void __launch_bounds__(256) k_adj_chunks(const __grid_constant__ AdjA
         for (int i = 0; i < TM; ++i)
 #pragma unroll
             for (int j = 0; j < TM; ++j)
-                if (own[i][j]) Rs[eo[i][j]] = cadd(Rs[eo[i][j]], acc[i][j]);
-        __syncthreads();
+                if (own[i][j]) Rs[eo[i][j]] = acc[i][j];
+    } else {
+        // ---- forward sweep: stored R_j for j in [s0, s1)
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TM; ++j)
+                if (own[i][j]) Rs[eo[i][j]] = a.pre[(size_t)blockIdx.x * dd + ge[i][j]];
+        for (long long st = s0; st < s1; ++st) {
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) a.Rbuf[(size_t)st * dd + ge[i][j]] = Rs[eo[i][j]];
+            if (st + 1 == s1) break;
+            assemble(st);
+            clenshaw_u();
+            // R <- U R = R + (U - I) R
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) {
+                        C u = acc[i][j];
+                        if (dg[i][j]) u.x -= (R)1;
+                        B1[eo[i][j]] = u;
+                    }
+            __syncthreads();
+            tile_gemm<C, TM>(acc, B1, Rs, d, ld, ty, tx);
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) Rs[eo[i][j]] = cadd(Rs[eo[i][j]], acc[i][j]);
+            __syncthreads();
+        }
     }
     __syncthreads();
 
@@ -207,13 +245,38 @@ __global__ void __launch_bounds__(256) k_adj_chunks(const __grid_constant__ AdjA
             if (own[i][j]) Ms[eo[i][j]] = acc[i][j];
 
     for (long long st = s1 - 1; st >= s0; --st) {
+        if (!a.reversible) {
 #pragma unroll
-        for (int i = 0; i < TM; ++i)
+            for (int i = 0; i < TM; ++i)
 #pragma unroll
-            for (int j = 0; j < TM; ++j)
-                if (own[i][j]) Rs[eo[i][j]] = a.Rbuf[(size_t)st * dd + ge[i][j]];
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) Rs[eo[i][j]] = a.Rbuf[(size_t)st * dd + ge[i][j]];
+        }
         assemble(st);
         __syncthreads();
+        if (a.reversible) {
+            // R_j = U_j^H R_(j+1) = R_(j+1) + (U_j - I)^H R_(j+1)
+            clenshaw_u();
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) {
+                        C u = acc[i][j];
+                        if (dg[i][j]) u.x -= (R)1;
+                        // conjugate transpose: element (r, c) of (U - I) goes to (c, r)
+                        B1[(tx + 16 * j) * ld + ty + 16 * i] = mk<C>(u.x, -u.y);
+                    }
+            __syncthreads();
+            tile_gemm<C, TM>(acc, B1, Rs, d, ld, ty, tx);
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j)
+                    if (own[i][j]) Rs[eo[i][j]] = cadd(Rs[eo[i][j]], acc[i][j]);
+            __syncthreads();
+        }
         // B_j = R_j M_j
         tile_gemm<C, TM>(acc, Rs, Ms, d, ld, ty, tx);
         // First Clenshaw order (b_M = J[M] I, derivative 0) needs own elements only:
@@ -437,7 +500,7 @@ static cudaError_t chunk_scan(bool fp64, int d, const void *S, long long nc, voi
 
 template <class R>
 static cudaError_t launch_adj_t(Ctx *c, const void *d_carr, unsigned pts, unsigned amps, const void *d_W,
-                                void *d_grad, int M, const double *J, double h, long long P, int nc,
+                                void *d_grad, int M, const double *J, double h, long long P, int nc, bool reversible,
                                 cudaStream_t st) {
     using C = cplx_t<R>;
     const int d = (int)c->dim;
@@ -475,7 +538,9 @@ static cudaError_t launch_adj_t(Ctx *c, const void *d_carr, unsigned pts, unsign
     a.pre = reinterpret_cast<const C *>(pre);
     a.suf = reinterpret_cast<const C *>(suf);
     a.W = static_cast<const C *>(d_W);
-    a.Rbuf = static_cast<C *>(c->X.ptr);
+    a.chunks = reinterpret_cast<const C *>(chunks);
+    a.reversible = reversible ? 1 : 0;
+    a.Rbuf = reversible ? nullptr : static_cast<C *>(c->X.ptr);
     a.tr = static_cast<C *>(c->aux.ptr);
     a.P = P;
     a.nchunks = nc;
@@ -528,12 +593,17 @@ Parament_ErrorCode run_vjp(Ctx *c, const void *d_carr, double dt, unsigned pts, 
     }
     const int nc = (int)std::max<long long>(1, std::min<long long>((long long)per_sm * c->num_sms, P));
     const size_t es = c->esize(), dd = (size_t)d * d;
+    // The order tables keep the truncation of every step exponential below
+    // the working precision, so U_j^H inverts U_j; a manual order may not.
+    const bool reversible = !c->manual;
     if (c->chunks.ensure(es * dd * nc) != cudaSuccess || c->work.ensure(4 * es * dd * nc) != cudaSuccess ||
-        c->X.ensure(es * dd * (size_t)P) != cudaSuccess ||
+        (!reversible && c->X.ensure(es * dd * (size_t)P) != cudaSuccess) ||
         c->aux.ensure(es * (size_t)P * std::max(1u, c->Ke)) != cudaSuccess)
         return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
-    cudaError_t e = c->fp64 ? launch_adj_t<double>(c, d_carr, pts, amps, d_W, d_grad, M, J.data(), h, P, nc, stream)
-                            : launch_adj_t<float>(c, d_carr, pts, amps, d_W, d_grad, M, J.data(), h, P, nc, stream);
+    cudaError_t e = c->fp64 ? launch_adj_t<double>(c, d_carr, pts, amps, d_W, d_grad, M, J.data(), h, P, nc,
+                                                   reversible, stream)
+                            : launch_adj_t<float>(c, d_carr, pts, amps, d_W, d_grad, M, J.data(), h, P, nc,
+                                                  reversible, stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return PARAMENT_STATUS_CUBLAS_FAILED;

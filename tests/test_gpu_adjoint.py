@@ -8,7 +8,11 @@ Checked against:
 - central finite differences (eps = 1e-4, FP64 equiprop) on 64 random entries
   of the d=32, K=6 fidelity workload;
 - the complex128 gradient, for the complex64 context;
-- the torch.autograd.Function binding.
+- the torch.autograd.Function binding;
+- the stored-checkpoint sweep (manual Chebyshev order) against the recomputing
+  one (automatic order) at the same order;
+- the device memory of the d=32, K=6, 16384-step gradient: no per-step
+  matrices.
 Tolerances are relative to the largest gradient entry.
 """
 import numpy as np
@@ -168,3 +172,55 @@ def test_vjp_errors(built_lib):
         ctx.set_hamiltonian(np.eye(49), np.eye(49))
         with pytest.raises(ValueError, match="Invalid value"):
             ctx.vjp(0.01, np.eye(49), np.zeros(3))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 1e-4)])
+def test_recomputed_and_stored_sweeps_agree(built_lib, precision, tol):
+    """The automatic order recomputes R_j = U_j^H R_(j+1) backward from the
+    chunk-end checkpoint; a manual order (here the same order) stores every
+    R_j of the forward sweep.  Both are the derivative of the same computed
+    propagator."""
+    import parament_gb300 as parament
+    from parament_gb300 import workloads
+    w = workloads.problem(12, 3, 2001, 1e-3, norm0=5.0, seed=4, magnus=True, quadrature=oracle.SIMPSON)
+    rng = np.random.default_rng(2)
+    W = rng.standard_normal((12, 12)) + 1j * rng.standard_normal((12, 12))
+    with parament.Parament(precision) as ctx:
+        ctx.set_hamiltonian(w["H0"], *w["H1"], use_magnus=True, quadrature_mode="simpson")
+        g_rec = ctx.vjp(w["dt"], W, *w["carr"].real)
+        M = ctx.last_iteration_cycles
+        ctx.set_iteration_cycles_manually(M)
+        g_sto = ctx.vjp(w["dt"], W, *w["carr"].real)
+    assert np.abs(g_rec - g_sto).max() <= tol * np.abs(g_sto).max()
+
+
+def test_gradient_memory_has_no_per_step_matrices(built_lib):
+    """d=32, K=6, 16384 steps, complex64: the context's device memory after a
+    gradient is the samples, the gradient, the per-step traces and a few
+    matrices per chunk (about one chunk per SM; the chunk boundaries are the
+    checkpoints) -- far below one d x d matrix per step."""
+    import torch
+
+    import parament_gb300 as parament
+    from parament_gb300 import workloads
+    w = workloads.adjoint_d32()
+    d, K, P, sc = 32, 6, w["P"], 8
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    free0 = torch.cuda.mem_get_info()[0]
+    with parament.Parament("fp32") as ctx:
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+        g = ctx.vjp(w["dt"], np.eye(d), *w["carr"].real)
+        held = ctx.device_memory_bytes
+        torch.cuda.synchronize()
+        used = free0 - torch.cuda.mem_get_info()[0]
+    per_step_mats = P * d * d * sc
+    io = K * P * sc + K * P * 4 + d * d * sc          # samples, gradient, seed
+    # traces (Ke = K here), the Hamiltonian stack, and five matrices per chunk
+    # (chunk product, prefix, suffix, two scan buffers) for at most eight
+    # resident CTAs per SM
+    budget = io + P * K * sc + (1 + K) * d * d * sc + 5 * 8 * nsm * d * d * sc
+    print(f"\ngradient d=32 P=16384: context holds {held / 2**20:.2f} MiB (budget {budget / 2**20:.2f} MiB, "
+          f"one matrix per step would be {per_step_mats / 2**20:.0f} MiB); driver reports {used / 2**20:.1f} MiB")
+    assert np.isfinite(g).all()
+    assert held <= budget
+    assert used < per_step_mats / 4
