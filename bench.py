@@ -49,13 +49,16 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--profile-case", default=None,
-                   choices=["split_c64", "plain_c64", "plain_c128", "large_dense_d512", "vjp_d32", "ensemble"],
+                   choices=["split_c64", "plain_c64", "plain_c128", "large_dense_d512", "split_large_d512", "vjp_d32",
+                            "ensemble"],
                    help="run one form twice (for ncu captures) and exit")
     p.add_argument("--forms", default="plain_c128,plain_c64,split_c64",
                    help="comma-separated forms to measure")
     p.add_argument("--large-c128-steps", type=int, default=4,
                    help="steps of the d=1024 complex128 workload to time (2048: the whole workload, ~3 min)")
     p.add_argument("--no-scipy-baseline", action="store_true")
+    p.add_argument("--no-large-fp64", action="store_true",
+                   help="skip the complex128 reference run of the d=512 workload (about a minute)")
     return p.parse_args()
 
 
@@ -399,43 +402,73 @@ def time_device(torch, ctx, w, carr, out, stream, K_steps, W_steps, flush=None):
     return sum(a.elapsed_time(b) for a, b in ts) / len(ts)
 
 
-def oracle_prefix_error(parament, w, precision, nsteps):
+def oracle_prefix_error(parament, w, precision, nsteps, split=False):
     """The first nsteps steps of a large workload on the GPU against the oracle
-    (complex64 contexts on the complex64-rounded inputs, against the oracle's
-    complex64-context arithmetic)."""
+    (complex64 contexts on the complex64-rounded inputs: the plain scheme
+    against the oracle's complex64-context arithmetic, the split form against
+    FP64)."""
     import oracle
     H0, H1, c = w["H0"], w["H1"], w["carr"][:, :nsteps]
     if precision == "fp32":
         H0, H1, c = (x.astype(np.complex64).astype(np.complex128) for x in (H0, H1, c))
     with parament.Parament(precision) as ctx:
+        if split:
+            ctx.set_precision_mode("split")
         ctx.set_hamiltonian(H0, *H1)
         U = ctx.equiprop(w["dt"], *c).astype(np.complex128)
-    Uo = oracle.equiprop(H0, H1, c, w["dt"], single=(precision == "fp32"), nthreads=os.cpu_count() or 1)[0]
+    Uo = oracle.equiprop(H0, H1, c, w["dt"], single=(precision == "fp32" and not split),
+                         nthreads=os.cpu_count() or 1)[0]
     return float(np.linalg.norm(U - Uo) / np.linalg.norm(Uo))
 
 
-def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, err_steps=12):
+def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, err_steps=12, fp64_check=True):
     """Large dense workload, complex64 d=512, K=8, ||H0|| = 20, smooth 8-mode
-    Fourier controls, all 8192 steps (steps x d^2 = 2^31): the tcgen05 3xTF32
-    GEMM path (kernel k_tc_cgemm).  The error column compares a prefix with
-    the oracle."""
+    Fourier controls, all 8192 steps (steps x d^2 = 2^31), in two forms: the
+    reference's plain complex64 scheme and the split form (double-float
+    first-order terms and chunk products, FP64 tree), both on the tcgen05
+    3xTF32 GEMM (k_tc_cgemm).  Errors: a prefix against the oracle, and the
+    whole run against the GPU's complex128 path."""
     from parament_gb300 import workloads
     w = workloads.large_dense(d=512, K=8, steps=8192)
+    for k in ("H0", "H1", "carr"):
+        w[k] = w[k].astype(np.complex64).astype(np.complex128)
     steps = w["P"]
-    ctx = parament.Parament("fp32")
-    ctx.set_hamiltonian(w["H0"], *w["H1"])
     carr = torch.tensor(w["carr"], dtype=torch.complex64, device="cuda")
     out = torch.empty((512, 512), dtype=torch.complex64, device="cuda")
-    ms = time_device(torch, ctx, w, carr, out, stream, K_steps, W_steps, flush)
-    M = ctx.last_iteration_cycles
-    ctx.destroy()
-    flops = steps * (M + 1) * 8.0 * 512 ** 3
-    return {"workload": f"large_dense d=512 K=8 complex64, all {steps} steps", "M": M, "ms": round(ms, 3),
-            "steps_per_s": round(steps / (ms * 1e-3), 1), "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
-            "kernel": "k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)",
-            "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, "fp32", err_steps),
-            "rel_err_prefix_steps": err_steps,
-            "scheme": "the reference's plain complex64 scheme (fp32 order table)"}
+    res = {"workload": f"large_dense d=512 K=8 complex64, all {steps} steps",
+           "kernel": "k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)"}
+    Us = {}
+    for form in ("plain_c64", "split_c64"):
+        ctx = parament.Parament("fp32")
+        if form == "split_c64":
+            ctx.set_precision_mode("split")
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+        ms = time_device(torch, ctx, w, carr, out, stream, K_steps, W_steps, flush)
+        M = ctx.last_iteration_cycles
+        Us[form] = out.cpu().numpy().astype(np.complex128)
+        ctx.destroy()
+        nprod = (M + 1) if form == "plain_c64" else (M - 3) // 2 + 3
+        flops = steps * (M + 1) * 8.0 * 512 ** 3
+        res[form] = {"M": M, "ms": round(ms, 3), "steps_per_s": round(steps / (ms * 1e-3), 1),
+                     "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
+                     "complex_products_per_step": nprod,
+                     "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, "fp32", err_steps,
+                                                                    split=(form == "split_c64")),
+                     "rel_err_prefix_steps": err_steps}
+    res["split_c64"]["scheme"] = ("split form: E = c0 + a1 Z (double-float) + Horner GEMMs, double-float chunk "
+                                  "running products, FP64 tree")
+    res["plain_c64"]["scheme"] = "the reference's plain complex64 scheme (fp32 order table)"
+    if fp64_check:
+        ctx = parament.Parament("fp64")
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+        t0 = time.perf_counter()
+        U128 = ctx.equiprop(w["dt"], *w["carr"]).astype(np.complex128)
+        res["fp64_reference_s"] = round(time.perf_counter() - t0, 2)
+        ctx.destroy()
+        for form in Us:
+            res[form]["rel_err_vs_gpu_c128_all_steps"] = float(np.linalg.norm(Us[form] - U128) /
+                                                                np.linalg.norm(U128))
+    return res
 
 
 def large_dense_c128_block(torch, parament, K_steps, W_steps, stream, steps=4, err_steps=3):
@@ -746,7 +779,8 @@ def run_ours(args, rank, world, local):
     except (ValueError, RuntimeError) as e:
         line["plain_d16"] = {"error": str(e)}
     try:
-        line["large_dense"] = large_dense_block(torch, parament, args.steps, args.warmup, flush, stream)
+        line["large_dense"] = large_dense_block(torch, parament, args.steps, args.warmup, flush, stream,
+                                                fp64_check=not args.no_large_fp64)
     except (ValueError, RuntimeError) as e:
         line["large_dense"] = {"error": str(e)}
     try:
@@ -787,9 +821,11 @@ def profile_case(args):
         ens.destroy()
         print("profile case", case, "done")
         return
-    if case == "large_dense_d512":
-        w = workloads.large_dense(d=512, K=8, steps=32)
+    if case in ("large_dense_d512", "split_large_d512"):
+        w = workloads.large_dense(d=512, K=8, steps=args.steps_per_prop if case == "split_large_d512" else 32)
         ctx = parament.Parament("fp32")
+        if case == "split_large_d512":
+            ctx.set_precision_mode("split")
         ctx.set_hamiltonian(w["H0"], *w["H1"])
     elif case == "vjp_d32":
         w = workloads.adjoint_d32(steps=args.steps_per_prop)

@@ -106,10 +106,13 @@ int select_cycles(bool fp64, double hnorm, double dt);
 void bessel_coeffs(int M, double x, double *J);
 long long num_steps(int quad, bool magnus, unsigned pts);
 
-// Split-precision form (complex64 contexts): order choice and propagation.
+// Split-precision form (complex64 contexts): order choice and propagation;
+// run_split_large serves d > 64 (split_large.cu).
+struct SplitArgs;
 int split_order(double hnorm, double h, long long P);
 Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned amps, double h, int M, long long P,
                              void *d_out, cudaStream_t stream);
+Parament_ErrorCode run_split_large(Ctx *c, const SplitArgs &a, double h, void *d_out, cudaStream_t stream);
 
 // Adjoint: d/du_k[i] Re Tr(W^H U) for real samples, d <= adj_max_dim.
 int adj_max_dim(bool fp64);

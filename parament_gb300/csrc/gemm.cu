@@ -22,7 +22,7 @@ struct GemmArgs {
     cplx_t<R> *Cout;
     long long sA, sB, sCin, sCout;
     cplx_t<R> alpha, diag;
-    R beta;
+    R beta, beta_im;
     int d, batch, tiles_per_row;
     int a_minus_identity;  // load A - I instead of A
 };
@@ -86,8 +86,10 @@ __global__ void __launch_bounds__(256) k_gemm(const __grid_constant__ GemmArgs<R
                 C v = cmul(g.alpha, acc[i][j]);
                 if (Cin) {
                     C o = Cin[e];
-                    v.x += g.beta * o.x;
-                    v.y += g.beta * o.y;
+                    v.x = fma(g.beta, o.x, v.x);
+                    v.y = fma(g.beta, o.y, v.y);
+                    v.x = fma(-g.beta_im, o.y, v.x);
+                    v.y = fma(g.beta_im, o.x, v.y);
                 }
                 if (r == c) v = cadd(v, g.diag);
                 Co[e] = v;
@@ -110,6 +112,7 @@ static cudaError_t run_gemm(const GemmLaunch &l) {
     g.alpha = mk<C>(l.alpha_re, l.alpha_im);
     g.diag = mk<C>(l.diag_re, l.diag_im);
     g.beta = (R)l.beta;
+    g.beta_im = (R)l.beta_im;
     g.d = l.d;
     g.batch = l.batch;
     g.tiles_per_row = (l.d + BT - 1) / BT;

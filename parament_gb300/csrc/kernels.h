@@ -45,8 +45,8 @@ size_t small_smem_bytes(bool fp64, int d, int Ke);
 cudaError_t launch_small_steps(const StepLaunch &a);
 
 // C_b = alpha * A_b B_b + beta * Cin_b + diag * I for b < batch (all d x d,
-// row-major; strides in elements).  Cin may alias Cout.  Cin may be null
-// when beta == 0.
+// row-major; strides in elements; beta = beta + i beta_im).  Cin may alias
+// Cout.  Cin may be null when beta == 0.
 struct GemmLaunch {
     bool fp64;
     int d;
@@ -62,6 +62,7 @@ struct GemmLaunch {
     double alpha_re, alpha_im;
     double beta;
     double diag_re, diag_im;
+    double beta_im;
     cudaStream_t stream;
     int num_sms;
     bool a_minus_identity;  // use A - I in place of A

@@ -525,7 +525,6 @@ static Parament_ErrorCode prepare_split_stack(Ctx *c) {
 Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned amps, double h, int M, long long P,
                              void *d_out, cudaStream_t stream) {
     const int d = (int)c->dim;
-    if (d > kSmallMaxDim) return PARAMENT_STATUS_INVALID_VALUE;
     if (M > kSplitMaxOrder || c->hnorm * h > kSplitMaxX) return PARAMENT_STATUS_SELECT_SMALLER_DT;
     Parament_ErrorCode r = prepare_split_stack(c);
     if (r != PARAMENT_STATUS_SUCCESS) return r;
@@ -549,6 +548,11 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
     a.magnus = c->magnus ? 1 : 0;
     a.hfac = h / 12.0;
     a.fault = c->d_fault;
+    a.wts = nullptr;
+    a.xplanes = nullptr;
+    a.chunks = nullptr;
+    a.nchunks = 0;
+    if (d > kSmallMaxDim) return run_split_large(c, a, h, d_out, stream);
     const size_t dd = (size_t)d * d;
     const bool tensor = split_tc_applies(d, (int)c->Ke, M);
     const void *fn = pick_split(d);

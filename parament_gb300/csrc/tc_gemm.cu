@@ -85,7 +85,7 @@ struct TcArgs {
     float2 *Cout;
     long long sA, sB, sCin, sCout;
     float2 alpha, diag;
-    float beta;
+    float beta, beta_im;
     int d, batch, tiles_n, a_minus_identity;
     int *fault;  // the calling context's counter of CTAs whose waits gave up
 };
@@ -326,10 +326,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_cgemm(const __grid_constan
                     const float xr = re[2 * jj], xi = im[2 * jj], yr = re[2 * jj + 1], yi = im[2 * jj + 1];
                     float4 o = make_float4(g.alpha.x * xr - g.alpha.y * xi, g.alpha.x * xi + g.alpha.y * xr,
                                            g.alpha.x * yr - g.alpha.y * yi, g.alpha.x * yi + g.alpha.y * yr);
-                    o.x += g.beta * ci[jj].x;
-                    o.y += g.beta * ci[jj].y;
-                    o.z += g.beta * ci[jj].z;
-                    o.w += g.beta * ci[jj].w;
+                    o.x = fmaf(g.beta, ci[jj].x, o.x);
+                    o.y = fmaf(g.beta, ci[jj].y, o.y);
+                    o.z = fmaf(g.beta, ci[jj].z, o.z);
+                    o.w = fmaf(g.beta, ci[jj].w, o.w);
+                    o.x = fmaf(-g.beta_im, ci[jj].y, o.x);
+                    o.y = fmaf(g.beta_im, ci[jj].x, o.y);
+                    o.z = fmaf(-g.beta_im, ci[jj].w, o.z);
+                    o.w = fmaf(g.beta_im, ci[jj].z, o.w);
                     if (row == col) o.x += g.diag.x, o.y += g.diag.y;
                     if (row == col + 1) o.z += g.diag.x, o.w += g.diag.y;
                     if (ok) *reinterpret_cast<float4 *>(Co + 16 * cc + 2 * jj) = o;
@@ -409,6 +413,7 @@ cudaError_t launch_tc_gemm(const GemmLaunch &l) {
     g.alpha = make_float2((float)l.alpha_re, (float)l.alpha_im);
     g.diag = make_float2((float)l.diag_re, (float)l.diag_im);
     g.beta = (float)l.beta;
+    g.beta_im = (float)l.beta_im;
     g.d = l.d;
     g.batch = l.batch;
     g.tiles_n = l.d / 128;
