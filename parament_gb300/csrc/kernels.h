@@ -87,6 +87,12 @@ bool split_tc_applies(int d, int Ke, int M);
 cudaError_t tree_product(bool fp64, int d, void *in, long long n, void *work, void *out, cudaStream_t stream,
                          int num_sms, int *levels = nullptr, int *fault = nullptr);
 
+// Ordered product of n complex64 chunk products (d <= 64) into the complex64
+// result through the double-float tree (split.cu): buf128 holds n, bufb
+// ceil(n / 2) d x d complex128-sized matrices.  *levels receives the launches.
+cudaError_t tree_df_c64(int d, const float2 *chunks, long long n, void *buf128, void *bufb, float2 *out,
+                        cudaStream_t stream, int *levels);
+
 // Large-d plain path: the steps [s0, s1) are assembled, exponentiated and
 // multiplied into one product written to `out`.  Buffers: X, B1, B2 each hold
 // `batch` matrices.

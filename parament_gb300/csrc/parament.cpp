@@ -293,7 +293,10 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
     cudaError_t e;
     if (d <= kSmallMaxDim) {
         const int nch = small_chunk_count(c->fp64, d, (int)c->Ke, P, c->num_sms);
-        if (c->chunks.ensure(es * dd * nch) != cudaSuccess || c->work.ensure(es * dd * nch) != cudaSuccess)
+        // complex64: the chunk products are combined by the double-float tree
+        // (complex128-sized buffers); complex128: by the FP64 tree.
+        if (c->chunks.ensure(es * dd * nch) != cudaSuccess || c->work.ensure(16 * dd * nch) != cudaSuccess ||
+            (!c->fp64 && c->X.ensure(16 * dd * ((nch + 1) / 2)) != cudaSuccess))
             return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
         StepLaunch l{};
         l.fp64 = c->fp64;
@@ -313,9 +316,12 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
         e = launch_small_steps(l);
         if (c->timing) cudaEventRecord(c->ev_stop, stream);
         int levels = 0;
-        if (e == cudaSuccess)
-            e = tree_product(c->fp64, d, c->chunks.ptr, nch, c->work.ptr, d_out, stream, c->num_sms, &levels,
+        if (e == cudaSuccess && c->fp64)
+            e = tree_product(true, d, c->chunks.ptr, nch, c->work.ptr, d_out, stream, c->num_sms, &levels,
                              c->d_fault);
+        else if (e == cudaSuccess)
+            e = tree_df_c64(d, static_cast<const float2 *>(c->chunks.ptr), nch, c->work.ptr, c->X.ptr,
+                            static_cast<float2 *>(d_out), stream, &levels);
         c->launches = 1 + levels;
     } else {
         // Batches of G steps held as X, b_(k+1), b_(k+2): 3 G d^2 elements, capped near 4 GiB.

@@ -392,6 +392,24 @@ static cudaError_t tree_df(int d, const double2 *chunks, long long n, float4 *bu
     return cudaGetLastError();
 }
 
+__global__ void k_c64_to_c128_chunks(const float2 *src, double2 *dst, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = make_double2(src[i].x, src[i].y);
+}
+
+cudaError_t tree_df_c64(int d, const float2 *chunks, long long n, void *buf128, void *bufb, float2 *out,
+                        cudaStream_t stream, int *levels) {
+    const long long m = (long long)d * d * n;
+    k_c64_to_c128_chunks<<<(int)std::min<long long>(4096, (m + 255) / 256), 256, 0, stream>>>(
+        chunks, static_cast<double2 *>(buf128), m);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = tree_df(d, static_cast<const double2 *>(buf128), n, static_cast<float4 *>(buf128), static_cast<float4 *>(bufb),
+                out, stream, levels);
+    *levels += 2;  // the conversions in and out
+    return e;
+}
+
 // Complex64 stack from the FP64 stack (round to nearest).
 __global__ void k_split_stack(const double2 *src, float2 *dst, long long n) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
