@@ -267,7 +267,10 @@ __global__ void __launch_bounds__(256, MINB) k_ensemble_class(const __grid_const
     }
 }
 
-// Ordered product of each problem's chunk products (later chunk on the left).
+// Ordered product of each problem's chunk products (later chunk on the left),
+// P <- A P formed as P + (A - I) P: a chunk product near the identity enters
+// the sums without its unit diagonal, so its small terms are not rounded
+// against 1 in FP32.
 template <class R>
 __global__ void __launch_bounds__(256) k_ensemble_reduce(const EnsProblem *probs, const cplx_t<R> *chunks,
                                                          cplx_t<R> *out) {
@@ -281,7 +284,11 @@ __global__ void __launch_bounds__(256) k_ensemble_reduce(const EnsProblem *probs
     for (int e = threadIdx.x; e < dd; e += blockDim.x) Ps[(e / d) * ld + e % d] = src[e];
     __syncthreads();
     for (int c = 1; c < p.nchunks; ++c) {
-        for (int e = threadIdx.x; e < dd; e += blockDim.x) As[(e / d) * ld + e % d] = src[(size_t)c * dd + e];
+        for (int e = threadIdx.x; e < dd; e += blockDim.x) {
+            C v = src[(size_t)c * dd + e];
+            if (e / d == e % d) v.x -= (R)1;
+            As[(e / d) * ld + e % d] = v;
+        }
         __syncthreads();
         C acc[4][4];
         tile_gemm<C, 4>(acc, As, Ps, d, ld, ty, tx);
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(256) k_ensemble_reduce(const EnsProblem *probs
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int r = ty + 16 * i, cc = tx + 16 * j;
-                if (r < d && cc < d) Ps[r * ld + cc] = acc[i][j];
+                if (r < d && cc < d) Ps[r * ld + cc] = cadd(Ps[r * ld + cc], acc[i][j]);
             }
         __syncthreads();
     }

@@ -293,6 +293,27 @@ cudaError_t launch_large_range(const LargeLaunch &l, int *launches) {
     return l.fp64 ? run_large<double>(l, launches) : run_large<float>(l, launches);
 }
 
+template <class S, class D>
+__global__ void k_convert(const S *src, D *dst, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        D v;
+        v.x = src[i].x;
+        v.y = src[i].y;
+        dst[i] = v;
+    }
+}
+
+cudaError_t convert_complex(bool to_fp64, const void *src, void *dst, long long n, cudaStream_t stream) {
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096));
+    if (to_fp64)
+        k_convert<float2, double2><<<blocks, 256, 0, stream>>>(static_cast<const float2 *>(src),
+                                                               static_cast<double2 *>(dst), n);
+    else
+        k_convert<double2, float2><<<blocks, 256, 0, stream>>>(static_cast<const double2 *>(src),
+                                                               static_cast<float2 *>(dst), n);
+    return cudaGetLastError();
+}
+
 template <class R>
 __global__ void k_fill_identity(cplx_t<R> *dst, int d, long long count, cplx_t<R> v) {
     const long long dd = (long long)d * d, n = dd * count;

@@ -87,6 +87,18 @@ bool split_tc_applies(int d, int Ke, int M);
 cudaError_t tree_product(bool fp64, int d, void *in, long long n, void *work, void *out, cudaStream_t stream,
                          int num_sms, int *levels = nullptr, int *fault = nullptr);
 
+// Fused plain-path kernel for 64 < d <= 128 (step_mid.cu): clusters of four
+// CTAs, one cluster per chunk of steps, writing one product per chunk into
+// `chunks` (l.nchunks = clusters).  mid_applies: whether the kernel's shared
+// memory holds this dimension and precision.
+bool mid_applies(bool fp64, int d, int Ke);
+int mid_chunk_count(int num_sms, long long P);
+cudaError_t launch_mid_steps(const StepLaunch &l);
+
+// n complex numbers converted between complex64 and complex128 (to_fp64:
+// complex64 -> complex128).
+cudaError_t convert_complex(bool to_fp64, const void *src, void *dst, long long n, cudaStream_t stream);
+
 // Ordered product of n complex64 chunk products (d <= 64) into the complex64
 // result through the double-float tree (split.cu): buf128 holds n, bufb
 // ceil(n / 2) d x d complex128-sized matrices.  *levels receives the launches.

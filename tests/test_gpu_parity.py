@@ -100,6 +100,28 @@ def test_large_dimension_path(built_lib, precision, d):
     assert relerr(U, Uo) < TOL[precision]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("d,magnus,n", [(96, True, 801), (128, False, 1500), (72, False, 37)])
+def test_cluster_resident_path(built_lib, precision, d, magnus, n):
+    """64 < d <= 128: clusters of four CTAs with the step in shared memory
+    (complex64 up to d = 128, complex128 up to d = 96; complex128 at d = 128
+    takes the batched path), against the oracle."""
+    rng = np.random.default_rng(d + n)
+    from parament_gb300.workloads import hermitian, sinusoid_controls
+    K = 3
+    H0 = hermitian(rng, d, 8.0)
+    H1 = np.stack([hermitian(rng, d, 1.0) for _ in range(K)])
+    carr = sinusoid_controls(rng, K, n, 1e-3)
+    mode = oracle.SIMPSON if magnus else oracle.NONE
+    U, M = run(H0, H1, list(carr), 1e-3, magnus, mode, precision)
+    if precision == "fp32":
+        H0, H1, carr = (x.astype(np.complex64).astype(np.complex128) for x in (H0, H1, carr))
+    Uo, Mo, _, _ = oracle.equiprop(H0, H1, carr, 1e-3, magnus=magnus, mode=mode, single=(precision == "fp32"),
+                                   nthreads=os.cpu_count())
+    assert M == Mo
+    assert relerr(U, Uo) < TOL[precision]
+
+
 @pytest.mark.parametrize("cycles", [1, 3, 5, 9, 21])
 def test_manual_cycles(built_lib, cycles):
     rng = np.random.default_rng(cycles)
