@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--profile-case", default=None,
                    choices=["split_c64", "plain_c64", "plain_c128", "large_dense_d512", "split_large_d512", "vjp_d32",
-                            "ensemble"],
+                            "ensemble", "mid_d128", "mid_d96_c128"],
                    help="run one form twice (for ncu captures) and exit")
     p.add_argument("--forms", default="plain_c128,plain_c64,split_c64",
                    help="comma-separated forms to measure")
@@ -821,7 +821,12 @@ def profile_case(args):
         ens.destroy()
         print("profile case", case, "done")
         return
-    if case in ("large_dense_d512", "split_large_d512"):
+    if case in ("mid_d128", "mid_d96_c128"):
+        d = 128 if case == "mid_d128" else 96
+        w = workloads.problem(d, 3, args.steps_per_prop, 1e-3, norm0=8.0, seed=5)
+        ctx = parament.Parament("fp32" if case == "mid_d128" else "fp64")
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+    elif case in ("large_dense_d512", "split_large_d512"):
         w = workloads.large_dense(d=512, K=8, steps=args.steps_per_prop if case == "split_large_d512" else 32)
         ctx = parament.Parament("fp32")
         if case == "split_large_d512":
@@ -837,7 +842,7 @@ def profile_case(args):
         ctx.set_hamiltonian(w["H0"], *w["H1"], use_magnus=True, quadrature_mode="simpson")
         if case == "split_c64":
             ctx.set_precision_mode("split")
-    ct = torch.complex128 if case == "plain_c128" else torch.complex64
+    ct = torch.complex128 if case in ("plain_c128", "mid_d96_c128") else torch.complex64
     carr = torch.tensor(w["carr"], dtype=ct, device="cuda")
     for _ in range(2):
         if case == "vjp_d32":
