@@ -435,8 +435,7 @@ def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, err_step
     steps = w["P"]
     carr = torch.tensor(w["carr"], dtype=torch.complex64, device="cuda")
     out = torch.empty((512, 512), dtype=torch.complex64, device="cuda")
-    res = {"workload": f"large_dense d=512 K=8 complex64, all {steps} steps",
-           "kernel": "k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)"}
+    res = {"workload": f"large_dense d=512 K=8 complex64, all {steps} steps"}
     Us = {}
     for form in ("plain_c64", "split_c64"):
         ctx = parament.Parament("fp32")
@@ -450,13 +449,15 @@ def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, err_step
         nprod = (M + 1) if form == "plain_c64" else (M - 3) // 2 + 3
         flops = steps * (M + 1) * 8.0 * 512 ** 3
         res[form] = {"M": M, "ms": round(ms, 3), "steps_per_s": round(steps / (ms * 1e-3), 1),
+                     "kernel": ("k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)" if form == "plain_c64"
+                                else "k_gemm<float> (FP32 SIMT) + k_sl_* elementwise"),
                      "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
                      "complex_products_per_step": nprod,
                      "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, "fp32", err_steps,
                                                                     split=(form == "split_c64")),
                      "rel_err_prefix_steps": err_steps}
     res["split_c64"]["scheme"] = ("split form: E = c0 + a1 Z (double-float) + Horner GEMMs, double-float chunk "
-                                  "running products, FP64 tree")
+                                  "running products, FP64 tree; every GEMM on the FP32 SIMT kernel (k_gemm)")
     res["plain_c64"]["scheme"] = "the reference's plain complex64 scheme (fp32 order table)"
     if fp64_check:
         ctx = parament.Parament("fp64")

@@ -67,6 +67,7 @@ struct GemmLaunch {
     int num_sms;
     bool a_minus_identity;  // use A - I in place of A
     int *fault;             // device counter of bounded waits that gave up (tensor-core kernel)
+    bool simt_only;         // FP32/FP64 SIMT kernel even where the tensor-core kernel applies
 };
 cudaError_t launch_gemm(const GemmLaunch &g);
 

@@ -15,9 +15,8 @@
 //     a float rounding of these repeats at every step and adds up coherently
 //     over thousands of steps;
 //   * p_j = sum_(n>=2) a_n Z_j^n is a few 1e-4 of the propagator and comes
-//     from GEMMs in FP32 arithmetic (tcgen05 3xTF32 products, k_tc_cgemm, for
-//     d % 128 == 0, d >= 256; the SIMT FP32 GEMM otherwise), by Horner's rule
-//     in Y = Z^2 with coefficients linear in Z:
+//     from FP32 GEMMs (the SIMT k_gemm), by Horner's rule in Y = Z^2 with
+//     coefficients linear in Z:
 //         R_top = a_(M-1) I + a_M Z,
 //         R_i   = R_(i+1) Y + a_(2i+3) Z + a_(2i+2) I,   p = R_0 Y;
 //   * the steps are multiplied into chunk products, one running product per
@@ -26,6 +25,14 @@
 //     with E_j P from a GEMM of the float parts: its rounding is relative to
 //     |E_j| |P|, so it does not grow with the distance of U from I;
 //   * the chunk products are combined by the FP64 tree (gemm.cu).
+//
+// Every GEMM of this form runs on the FP32 SIMT kernel, not on the tcgen05
+// 3xTF32 kernel (k_tc_cgemm): the tensor core's FP32 accumulation rounds
+// with a bias, and at d = 512 over 700 steps the form measured 8.5e-6
+// against complex128 with every GEMM on the tensor cores, 5.8e-7 with only
+// the Horner GEMMs there, and 3.3e-8 with none -- the error repeats at every
+// step and the bar is 1e-6.  (The d = 64 split kernel avoids it with integer
+// bf16 slices, whose sums the accumulators hold exactly.)
 //
 // Every chunk advances by one step per round: a round assembles Z for the
 // active chunks' next steps (one batch item per chunk), runs the Horner GEMMs
@@ -225,6 +232,7 @@ Parament_ErrorCode run_split_large(Ctx *c, const SplitArgs &a, double h, void *d
     auto gemm = [&](const float2 *A, const float2 *B, const float2 *Cin, float2 *Cout, int batch, double2 beta,
                     double2 diag) {
         GemmLaunch g{};
+        g.simt_only = true;
         g.fp64 = false;
         g.d = d;
         g.batch = batch;

@@ -396,7 +396,7 @@ static bool make_map(CUtensorMap *m, const void *base, int d, long long stride, 
 }
 
 bool tc_gemm_applies(const GemmLaunch &l) {
-    return !l.fp64 && l.d >= 256 && l.d % 128 == 0 && !tc_disabled() && aligned16(l.A, l.strideA) &&
+    return !l.fp64 && !l.simt_only && l.d >= 256 && l.d % 128 == 0 && !tc_disabled() && aligned16(l.A, l.strideA) &&
            aligned16(l.B, l.strideB) && aligned16(l.Cin, l.strideCin) && aligned16(l.Cout, l.strideCout);
 }
 
