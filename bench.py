@@ -540,6 +540,34 @@ def plain_d16_block(torch, parament, K_steps, W_steps, flush, stream, lib_peaks)
             "rel_err_vs_oracle": float(np.linalg.norm(U - Uo) / np.linalg.norm(Uo))}
 
 
+def mid_block(torch, parament, K_steps, W_steps, flush, stream, steps=16384):
+    """64 < d <= 128 on the cluster kernel (k_mid_steps): d=128 complex64 and
+    d=96 complex128, K=3, NONE quadrature, ||H0|| = 8, `steps` steps; device
+    time per propagation, algorithmic TFLOP/s (8 d^3 (M+1) + 8 K d^2 per
+    step) and a 64-step prefix against the oracle."""
+    from parament_gb300 import workloads
+    out = {}
+    for d, prec in ((128, "fp32"), (96, "fp64")):
+        w = workloads.problem(d, 3, steps, 1e-3, norm0=8.0, seed=5)
+        ctx = parament.Parament(prec)
+        ctx.set_hamiltonian(w["H0"], *w["H1"])
+        ct = torch.complex128 if prec == "fp64" else torch.complex64
+        carr = torch.tensor(w["carr"], dtype=ct, device="cuda")
+        o = torch.empty((d, d), dtype=ct, device="cuda")
+        ms = time_device(torch, ctx, w, carr, o, stream, K_steps, W_steps, flush)
+        M = ctx.last_iteration_cycles
+        launches = int(getattr(parament.paramentlib.lib, "Parament_lastLaunchCount" +
+                               ("_fp64" if prec == "fp64" else ""))(ctx._handle))
+        ctx.destroy()
+        fl = algorithmic_flops_per_step(d, M, 3) * steps
+        out[f"d{d}_{'c128' if prec == 'fp64' else 'c64'}"] = {
+            "M": M, "ms": round(ms, 3), "steps_per_s": round(steps / (ms * 1e-3), 1),
+            "algorithmic_tflops": round(fl / (ms * 1e-3) / 1e12, 2), "launches": launches,
+            "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, prec, 64), "rel_err_prefix_steps": 64}
+    out["workload"] = f"K=3 NONE ||H0||=8, {steps} steps; k_mid_steps (clusters of four CTAs)"
+    return out
+
+
 def scipy_block(w16, w64):
     """The NumPy/SciPy FP64 expm-product of the same scheme on the host cores:
     one process (one BLAS thread) and one process per core over contiguous
@@ -779,6 +807,10 @@ def run_ours(args, rank, world, local):
         line["plain_d16"] = plain_d16_block(torch, parament, args.steps, args.warmup, flush, stream, lib_peaks)
     except (ValueError, RuntimeError) as e:
         line["plain_d16"] = {"error": str(e)}
+    try:
+        line["mid_d"] = mid_block(torch, parament, args.steps, args.warmup, flush, stream)
+    except (ValueError, RuntimeError) as e:
+        line["mid_d"] = {"error": str(e)}
     try:
         line["large_dense"] = large_dense_block(torch, parament, args.steps, args.warmup, flush, stream,
                                                 fp64_check=not args.no_large_fp64)
