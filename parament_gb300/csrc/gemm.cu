@@ -125,7 +125,8 @@ static cudaError_t run_gemm(const GemmLaunch &l) {
 cudaError_t launch_gemm(const GemmLaunch &l) {
     if (l.batch <= 0) return cudaSuccess;
     if (l.d < 1) return cudaErrorInvalidValue;
-    if (tc_gemm_applies(l)) return launch_tc_gemm(l);
+    if (l.exact && l.scales && oz_gemm_applies(l)) return launch_oz_gemm(l, l.scales);
+    if (!l.exact && tc_gemm_applies(l)) return launch_tc_gemm(l);
     // Largest tile that still gives two CTAs per SM; small products get small tiles.
     auto tiles = [&](int bt) { long long t = (l.d + bt - 1) / bt; return t * t * (long long)l.batch; };
     int bt = 16;

@@ -68,8 +68,19 @@ struct GemmLaunch {
     bool a_minus_identity;  // use A - I in place of A
     int *fault;             // device counter of bounded waits that gave up (tensor-core kernel)
     bool simt_only;         // FP32/FP64 SIMT kernel even where the tensor-core kernel applies
+    // complex64 products without a rounding bias: the exact sliced tensor-core
+    // kernel (tc_ozaki.cu) where it applies, the FP32 SIMT kernel otherwise.
+    // `scales` is its scratch: oz_scale_ints(g) ints (null: SIMT).
+    bool exact;
+    int *scales;
 };
 cudaError_t launch_gemm(const GemmLaunch &g);
+
+// Exact sliced complex64 GEMM (integer bf16 slices, tcgen05): d % 64 == 0,
+// 128 <= d <= 2048, no A - I.
+bool oz_gemm_applies(const GemmLaunch &g);
+size_t oz_scale_ints(const GemmLaunch &g);
+cudaError_t launch_oz_gemm(const GemmLaunch &g, int *scales);
 
 // tcgen05 tensor-core complex64 GEMM (3xTF32), used by launch_gemm for
 // complex64 with d >= 256 and d % 128 == 0.  A CTA whose bounded waits gave

@@ -193,7 +193,10 @@ Parament_ErrorCode run_split_large(Ctx *c, const SplitArgs &a, double h, void *d
     const size_t mat = sizeof(float2) * (size_t)dd * nch;
     // zhi zlo y r0 r1 p ehi elo dprod phi plo
     constexpr int kBufs = 11;
-    if (c->xplanes.ensure(kBufs * mat) != cudaSuccess ||
+    // Scratch of the exact GEMM: exponents of the row / column maxima of the
+    // operands of one batched product (two operands of nch items).
+    const size_t scale_bytes = sizeof(int) * 2 * (size_t)nch * d;
+    if (c->xplanes.ensure(kBufs * mat + scale_bytes) != cudaSuccess ||
         c->chunks.ensure(sizeof(double2) * (size_t)dd * nch) != cudaSuccess ||
         c->work.ensure(sizeof(double2) * (size_t)dd * nch) != cudaSuccess ||
         c->aux.ensure(sizeof(double2) * (size_t)dd) != cudaSuccess)
@@ -201,6 +204,7 @@ Parament_ErrorCode run_split_large(Ctx *c, const SplitArgs &a, double h, void *d
     float2 *buf[kBufs];
     for (int i = 0; i < kBufs; ++i)
         buf[i] = reinterpret_cast<float2 *>(static_cast<char *>(c->xplanes.ptr) + (size_t)i * mat);
+    int *scales = reinterpret_cast<int *>(static_cast<char *>(c->xplanes.ptr) + (size_t)kBufs * mat);
     float2 *zhi = buf[0], *zlo = buf[1], *y = buf[2], *rb[2] = {buf[3], buf[4]}, *pp = buf[5], *ehi = buf[6],
            *elo = buf[7], *dprod = buf[8], *phi = buf[9], *plo = buf[10];
     // Coefficients in Z = h X: a_n = mu_n / h^n.
@@ -232,7 +236,8 @@ Parament_ErrorCode run_split_large(Ctx *c, const SplitArgs &a, double h, void *d
     auto gemm = [&](const float2 *A, const float2 *B, const float2 *Cin, float2 *Cout, int batch, double2 beta,
                     double2 diag) {
         GemmLaunch g{};
-        g.simt_only = true;
+        g.exact = true;
+        g.scales = scales;
         g.fp64 = false;
         g.d = d;
         g.batch = batch;
