@@ -15,8 +15,7 @@
 //     a float rounding of these repeats at every step and adds up coherently
 //     over thousands of steps;
 //   * p_j = sum_(n>=2) a_n Z_j^n is a few 1e-4 of the propagator and comes
-//     from FP32 GEMMs (the SIMT k_gemm), by Horner's rule in Y = Z^2 with
-//     coefficients linear in Z:
+//     from GEMMs by Horner's rule in Y = Z^2 with coefficients linear in Z:
 //         R_top = a_(M-1) I + a_M Z,
 //         R_i   = R_(i+1) Y + a_(2i+3) Z + a_(2i+2) I,   p = R_0 Y;
 //   * the steps are multiplied into chunk products, one running product per
@@ -26,13 +25,14 @@
 //     |E_j| |P|, so it does not grow with the distance of U from I;
 //   * the chunk products are combined by the FP64 tree (gemm.cu).
 //
-// Every GEMM of this form runs on the FP32 SIMT kernel, not on the tcgen05
-// 3xTF32 kernel (k_tc_cgemm): the tensor core's FP32 accumulation rounds
-// with a bias, and at d = 512 over 700 steps the form measured 8.5e-6
-// against complex128 with every GEMM on the tensor cores, 5.8e-7 with only
-// the Horner GEMMs there, and 3.3e-8 with none -- the error repeats at every
-// step and the bar is 1e-6.  (The d = 64 split kernel avoids it with integer
-// bf16 slices, whose sums the accumulators hold exactly.)
+// The GEMMs ask for products without a rounding bias (GemmLaunch::exact):
+// the exact sliced tensor-core kernel (tc_ozaki.cu: integer bf16 slices, FP32
+// accumulators that never round) for d % 64 == 0 up to 1536, the FP32 SIMT
+// kernel otherwise.  Not the 3xTF32 kernel (k_tc_cgemm): the tensor core's FP32
+// accumulation rounds with a bias, and at d = 512 over 700 steps the form
+// measured 8.5e-6 against complex128 with every GEMM there, 5.8e-7 with only
+// the Horner GEMMs there, 3.3e-8 on the SIMT kernel and 2.5e-8 on the exact
+// kernel -- the error repeats at every step and the bar is 1e-6.
 //
 // Every chunk advances by one step per round: a round assembles Z for the
 // active chunks' next steps (one batch item per chunk), runs the Horner GEMMs

@@ -33,8 +33,8 @@
 // lands in tensor-memory lanes 0..63, Im C in 64..127.
 //
 // One CTA of 512 threads per SM walks the (item, block row, block column)
-// units; per K block every thread loads 16 values of A and of B (one plane
-// of one row, 16 columns), slices them into shared memory, and one thread
+// units; per K block every thread loads 8 complex values of A and of B (one
+// row, 8 columns), slices them into shared memory, and one thread
 // issues the 120 MMAs (15 slice products of 8 MMAs); the next K block's values
 // are loaded while those run.  Every wait on the tensor core is bounded.
 #include <stdlib.h>
@@ -127,15 +127,18 @@ __device__ __forceinline__ void oz_peel(float (&t)[8], float (&q)[kOzSlices][8])
         }
 }
 
-// This thread's 16 values of one plane: row `row` of a row-major complex
-// matrix, columns col0 .. col0 + 15.
-__device__ __forceinline__ void oz_load16(const float2 *m, int d, int row, int col0, int plane, float (&v)[16]) {
+// Eight complex values of a row-major matrix: row `row`, columns col0 ..
+// col0 + 7 (64 contiguous bytes; eight threads cover a row of a K block, so a
+// warp reads four rows of 512 bytes), split into the two planes.
+__device__ __forceinline__ void oz_load8(const float2 *m, int d, int row, int col0, float (&re)[8], float (&im)[8]) {
     const float4 *p = reinterpret_cast<const float4 *>(m + (size_t)row * d + col0);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < 4; ++i) {
         const float4 x = __ldg(p + i);
-        v[2 * i] = plane ? x.y : x.x;
-        v[2 * i + 1] = plane ? x.w : x.z;
+        re[2 * i] = x.x;
+        im[2 * i] = x.y;
+        re[2 * i + 1] = x.z;
+        im[2 * i + 1] = x.w;
     }
 }
 
@@ -191,27 +194,39 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_cgemm(const __grid_constan
         const int ia = g.sA > 0 ? b : 0, ib = g.sB > 0 ? b : 0;
         const float2 *A = g.A + (size_t)ia * g.sA;
         const float2 *B = g.B + (size_t)ib * g.sB;
-        const int rowA = I * 64 + r;
-        const float sa = oz_pow2(5 - g.ea[(size_t)ia * d + rowA]);
-        float sb[16];
+        // Slicing: thread (lr, lg) takes row lr of the K block of A (and of B),
+        // complex columns 8 lg .. 8 lg + 7, both planes.
+        const int lr = tid >> 3, lg = tid & 7;
+        const float sa = oz_pow2(5 - g.ea[(size_t)ia * d + I * 64 + lr]);
+        float sb[8];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) sb[j] = oz_pow2(5 - g.eb[(size_t)ib * d + J * 64 + c0 + j]);
-        float av[16], bv[16];
-        oz_load16(A, d, rowA, c0, p, av);
-        oz_load16(B, d, r, J * 64 + c0, p, bv);
+        for (int j = 0; j < 8; ++j) sb[j] = oz_pow2(5 - g.eb[(size_t)ib * d + J * 64 + 8 * lg + j]);
+        float ar[8], ai[8], br[8], bi[8];
+        oz_load8(A, d, I * 64 + lr, 8 * lg, ar, ai);
+        oz_load8(B, d, lr, J * 64 + 8 * lg, br, bi);
         for (int kb = 0; kb < nblk; ++kb) {
             // Slices of this K block into shared memory.
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
+            {
                 float t[8], q[kOzSlices][8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) t[j] = av[8 * h + j] * sa;
+                for (int j = 0; j < 8; ++j) t[j] = ar[j] * sa;
                 oz_peel(t, q);
-                oz::store_a8<kOzSlices>(SA, r, c0 + 8 * h, p, q);
+                oz::store_a8<kOzSlices>(SA, lr, 8 * lg, 0, q);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) t[j] = bv[8 * h + j] * sb[8 * h + j];
+                for (int j = 0; j < 8; ++j) t[j] = ai[j] * sa;
                 oz_peel(t, q);
-                const uint32_t off = oz::sw(64 * p + r, c0 + 8 * h);
+                oz::store_a8<kOzSlices>(SA, lr, 8 * lg, 1, q);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) t[j] = br[j] * sb[j];
+                oz_peel(t, q);
+                uint32_t off = oz::sw(lr, 8 * lg);
+#pragma unroll
+                for (int s = 0; s < kOzSlices; ++s)
+                    *reinterpret_cast<uint4 *>(SB + s * oz::kBSlice + off) = oz::pack8(q[s]);
+#pragma unroll
+                for (int j = 0; j < 8; ++j) t[j] = bi[j] * sb[j];
+                oz_peel(t, q);
+                off = oz::sw(64 + lr, 8 * lg);
 #pragma unroll
                 for (int s = 0; s < kOzSlices; ++s)
                     *reinterpret_cast<uint4 *>(SB + s * oz::kBSlice + off) = oz::pack8(q[s]);
@@ -244,8 +259,8 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_cgemm(const __grid_constan
             }
             // The next K block's values load while the tensor core runs.
             if (kb + 1 < nblk) {
-                oz_load16(A, d, rowA, (kb + 1) * 64 + c0, p, av);
-                oz_load16(B, d, (kb + 1) * 64 + r, J * 64 + c0, p, bv);
+                oz_load8(A, d, I * 64 + lr, (kb + 1) * 64 + 8 * lg, ar, ai);
+                oz_load8(B, d, (kb + 1) * 64 + lr, J * 64 + 8 * lg, br, bi);
             }
             ok = tc::mbar_wait(&bar, ncommit & 1, kOzWait);
             ++ncommit;
@@ -260,7 +275,7 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_cgemm(const __grid_constan
 #pragma unroll
             for (int L = 0; L < kOzSlices; ++L) oz_ld16(tm + 64u * L, lv[L]);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            const int era = g.ea[(size_t)ia * d + rowA];
+            const int era = g.ea[(size_t)ia * d + I * 64 + r];
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 float v = lv[kOzSlices - 1][j];
