@@ -450,14 +450,14 @@ def large_dense_block(torch, parament, K_steps, W_steps, flush, stream, err_step
         flops = steps * (M + 1) * 8.0 * 512 ** 3
         res[form] = {"M": M, "ms": round(ms, 3), "steps_per_s": round(steps / (ms * 1e-3), 1),
                      "kernel": ("k_tc_cgemm (tcgen05 kind::tf32, 3xTF32 split products)" if form == "plain_c64"
-                                else "k_gemm<float> (FP32 SIMT) + k_sl_* elementwise"),
+                                else "k_oz_cgemm (tcgen05 kind::f16, exact 6-bit bf16 slices) + k_sl_* elementwise"),
                      "algorithmic_tflops": round(flops / (ms * 1e-3) / 1e12, 2),
                      "complex_products_per_step": nprod,
                      "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, "fp32", err_steps,
                                                                     split=(form == "split_c64")),
                      "rel_err_prefix_steps": err_steps}
     res["split_c64"]["scheme"] = ("split form: E = c0 + a1 Z (double-float) + Horner GEMMs, double-float chunk "
-                                  "running products, FP64 tree; every GEMM on the FP32 SIMT kernel (k_gemm)")
+                                  "running products, FP64 tree; GEMMs on the exact sliced tensor-core kernel")
     res["plain_c64"]["scheme"] = "the reference's plain complex64 scheme (fp32 order table)"
     if fp64_check:
         ctx = parament.Parament("fp64")
