@@ -541,10 +541,10 @@ def plain_d16_block(torch, parament, K_steps, W_steps, flush, stream, lib_peaks)
 
 
 def mid_block(torch, parament, K_steps, W_steps, flush, stream, steps=16384):
-    """64 < d <= 128 on the cluster kernel (k_mid_steps): d=128 complex64 and
-    d=96 complex128, K=3, NONE quadrature, ||H0|| = 8, `steps` steps; device
-    time per propagation, algorithmic TFLOP/s (8 d^3 (M+1) + 8 K d^2 per
-    step) and a 64-step prefix against the oracle."""
+    """64 < d <= 128: d=128 complex64 and d=96 complex128, K=3, NONE
+    quadrature, ||H0|| = 8, `steps` steps; device time per propagation,
+    algorithmic TFLOP/s (8 d^3 (M+1) + 8 K d^2 per step) and a 64-step prefix
+    against the oracle."""
     from parament_gb300 import workloads
     out = {}
     for d, prec in ((128, "fp32"), (96, "fp64")):
@@ -564,7 +564,8 @@ def mid_block(torch, parament, K_steps, W_steps, flush, stream, steps=16384):
             "M": M, "ms": round(ms, 3), "steps_per_s": round(steps / (ms * 1e-3), 1),
             "algorithmic_tflops": round(fl / (ms * 1e-3) / 1e12, 2), "launches": launches,
             "rel_err_vs_oracle_prefix": oracle_prefix_error(parament, w, prec, 64), "rel_err_prefix_steps": 64}
-    out["workload"] = f"K=3 NONE ||H0||=8, {steps} steps; k_mid_steps (clusters of four CTAs)"
+    out["workload"] = (f"K=3 NONE ||H0||=8, {steps} steps; the default path for 64 < d <= 128 (batched GEMMs; "
+                       f"the cluster-resident k_mid_steps serves when the batch buffers cannot be allocated)")
     return out
 
 

@@ -48,15 +48,18 @@ void DevBuf::release() {
 }
 
 // Host-side fault injection: PARAMENT_FAIL_ALLOC_AFTER=n makes the (n+1)-th
-// device allocation of this process report failure, so the allocation-failure
-// paths can be tested without exhausting the GPU.
+// device allocation of this process (and only that one) report failure, so
+// the allocation-failure paths can be tested without exhausting the GPU.
 bool fault_inject_alloc() {
     static long long budget = [] {
         const char *v = getenv("PARAMENT_FAIL_ALLOC_AFTER");
         return v ? atoll(v) : -1LL;
     }();
     if (budget < 0) return false;
-    if (budget == 0) return true;
+    if (budget == 0) {
+        budget = -1;  // that one allocation fails; later ones proceed
+        return true;
+    }
     --budget;
     return false;
 }
@@ -323,44 +326,6 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
             e = tree_df_c64(d, static_cast<const float2 *>(c->chunks.ptr), nch, c->work.ptr, c->X.ptr,
                             static_cast<float2 *>(d_out), stream, &levels);
         c->launches = 1 + levels;
-    } else if (mid_applies(c->fp64, d, (int)c->Ke)) {
-        // 64 < d <= 128: clusters of four CTAs with the step resident in their
-        // shared memory; the chunk products are combined by the FP64 tree.
-        const int nch = mid_chunk_count(c->num_sms, P);
-        if (c->chunks.ensure(es * dd * nch) != cudaSuccess || c->work.ensure(16 * dd * nch) != cudaSuccess ||
-            c->X.ensure(16 * dd * nch) != cudaSuccess || c->aux.ensure(16 * dd) != cudaSuccess)
-            return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
-        StepLaunch l{};
-        l.fp64 = c->fp64;
-        l.d = d;
-        l.Ke = (int)c->Ke;
-        l.w = w;
-        l.M = M;
-        l.J = J.data();
-        l.s = s;
-        l.stack = c->stack.ptr;
-        l.carr = d_carr;
-        l.chunks = c->chunks.ptr;
-        l.P = P;
-        l.nchunks = nch;
-        l.stream = stream;
-        if (c->timing) cudaEventRecord(c->ev_start, stream);
-        e = launch_mid_steps(l);
-        if (c->timing) cudaEventRecord(c->ev_stop, stream);
-        int levels = 0;
-        if (c->fp64) {
-            if (e == cudaSuccess)
-                e = tree_product(true, d, c->chunks.ptr, nch, c->work.ptr, d_out, stream, c->num_sms, &levels,
-                                 c->d_fault);
-            c->launches = 1 + levels;
-        } else {
-            if (e == cudaSuccess) e = convert_complex(true, c->chunks.ptr, c->work.ptr, dd * nch, stream);
-            if (e == cudaSuccess)
-                e = tree_product(true, d, c->work.ptr, nch, c->X.ptr, c->aux.ptr, stream, c->num_sms, &levels,
-                                 c->d_fault);
-            if (e == cudaSuccess) e = convert_complex(false, c->aux.ptr, d_out, dd, stream);
-            c->launches = 3 + levels;
-        }
     } else {
         // Batches of G steps held as X, b_(k+1), b_(k+2): 3 G d^2 elements, capped near 4 GiB.
         const size_t per = 3 * es * dd;
@@ -369,8 +334,54 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
         const long long nb = (P + G - 1) / G;
         if (c->X.ensure(es * dd * G) != cudaSuccess || c->B1.ensure(es * dd * G) != cudaSuccess ||
             c->B2.ensure(es * dd * G) != cudaSuccess || c->chunks.ensure(es * dd * nb) != cudaSuccess ||
-            c->work.ensure(es * dd * nb) != cudaSuccess)
-            return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+            c->work.ensure(es * dd * nb) != cudaSuccess) {
+            if (!mid_applies(c->fp64, d, (int)c->Ke)) return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+            // 64 < d <= 128 (96 in complex128) without room for the batches:
+            // clusters of four CTAs with the step resident in their shared
+            // memory, one d x d product per cluster (the batched path is about
+            // twice as fast where its buffers fit); the chunk products are
+            // combined by the FP64 tree.
+            const int nch = mid_chunk_count(c->num_sms, P);
+            if (c->chunks.ensure(es * dd * nch) != cudaSuccess || c->work.ensure(16 * dd * nch) != cudaSuccess ||
+                c->X.ensure(16 * dd * nch) != cudaSuccess || c->aux.ensure(16 * dd) != cudaSuccess)
+                return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+            StepLaunch l{};
+            l.fp64 = c->fp64;
+            l.d = d;
+            l.Ke = (int)c->Ke;
+            l.w = w;
+            l.M = M;
+            l.J = J.data();
+            l.s = s;
+            l.stack = c->stack.ptr;
+            l.carr = d_carr;
+            l.chunks = c->chunks.ptr;
+            l.P = P;
+            l.nchunks = nch;
+            l.stream = stream;
+            if (c->timing) cudaEventRecord(c->ev_start, stream);
+            e = launch_mid_steps(l);
+            if (c->timing) cudaEventRecord(c->ev_stop, stream);
+            int levels = 0;
+            if (c->fp64) {
+                if (e == cudaSuccess)
+                    e = tree_product(true, d, c->chunks.ptr, nch, c->work.ptr, d_out, stream, c->num_sms, &levels,
+                                     c->d_fault);
+                c->launches = 1 + levels;
+            } else {
+                if (e == cudaSuccess) e = convert_complex(true, c->chunks.ptr, c->work.ptr, dd * nch, stream);
+                if (e == cudaSuccess)
+                    e = tree_product(true, d, c->work.ptr, nch, c->X.ptr, c->aux.ptr, stream, c->num_sms, &levels,
+                                     c->d_fault);
+                if (e == cudaSuccess) e = convert_complex(false, c->aux.ptr, d_out, dd, stream);
+                c->launches = 3 + levels;
+            }
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return PARAMENT_STATUS_CUBLAS_FAILED;
+            }
+            return PARAMENT_STATUS_SUCCESS;
+        }
         LargeLaunch l{};
         l.fp64 = c->fp64;
         l.d = d;
