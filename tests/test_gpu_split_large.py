@@ -1,9 +1,10 @@
 """The split-precision complex64 form for d > 64 (split_large.cu).
 
 Its parity bar is the FP64 oracle on the complex64-rounded inputs: relative
-Frobenius error <= 1e-6, as for the d <= 64 split form.  Cases: d = 96 (SIMT
-FP32 GEMMs) with Magnus and Simpson, d = 256 and 384 (tcgen05 3xTF32 GEMMs)
-in the other quadratures, uneven chunk lengths, and the d=512, K=8 large dense
+Frobenius error <= 1e-6, as for the d <= 64 split form.  Cases: d = 96 (FP32
+SIMT GEMMs) with Magnus and Simpson, d = 192, 256 and 384 (the exact sliced
+tensor-core GEMM) in the other quadratures, uneven chunk lengths, d = 1024
+(sixteen K blocks) against the complex128 path, and the d=512, K=8 large dense
 workload -- a prefix against the oracle and all 8192 steps against the GPU's
 complex128 path (itself held to 1e-10 of the oracle).
 """
@@ -39,7 +40,7 @@ def run(H0, H1, carr, dt, magnus=False, mode=0, precision="fp32", split=True):
 
 
 @pytest.mark.parametrize("d,K,n,magnus,mode", [(96, 2, 101, True, oracle.SIMPSON), (256, 3, 211, False, oracle.NONE),
-                                               (384, 2, 77, False, oracle.MIDPOINT)])
+                                               (384, 2, 77, False, oracle.MIDPOINT), (192, 2, 301, True, oracle.SIMPSON)])
 def test_split_large_against_oracle(built_lib, d, K, n, magnus, mode):
     from parament_gb300.workloads import hermitian, sinusoid_controls
     rng = np.random.default_rng(d)
@@ -79,4 +80,17 @@ def test_split_large_dense_full_length(built_lib, dense512):
     U128, _ = run(w["H0"], w["H1"], list(w["carr"]), w["dt"], precision="fp64", split=False)
     e = relerr(U, U128)
     print(f"\nsplit d=512 K=8 8192 steps (M={M}): rel err vs complex128 {e:.3e}")
+    assert e < 1e-6
+
+
+def test_split_large_d1024_against_complex128(built_lib):
+    """d=1024 (sixteen K blocks of the exact sliced GEMM), 64 steps, against
+    the complex128 path on the same complex64-rounded inputs."""
+    from parament_gb300 import workloads
+    w = workloads.large_dense(d=1024, K=4, steps=64)
+    H0, H1, carr = c64(w["H0"]), c64(w["H1"]), c64(w["carr"])
+    U, M = run(H0, H1, list(carr), w["dt"])
+    U128, _ = run(H0, H1, list(carr), w["dt"], precision="fp64", split=False)
+    e = relerr(U, U128)
+    print(f"\nsplit d=1024 K=4 64 steps (M={M}): rel err vs complex128 {e:.3e}")
     assert e < 1e-6
