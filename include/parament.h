@@ -126,11 +126,13 @@ PARAMENT_API void device_info(void);
  *                              first-order term in double-float (pairs of
  *                              floats), the higher powers as sliced products
  *                              (bf16 slices of integers, accumulated exactly on
- *                              the tensor cores) at d = 64 or FP32 products at
- *                              d < 64; each chunk of consecutive steps is
- *                              multiplied into a double-float running product
- *                              (sliced products again at d = 64) and the chunk
- *                              products are combined by a double-float tree.
+ *                              the tensor cores) at d = 64 and at d > 64 with
+ *                              d % 64 == 0, FP32 products otherwise; each chunk
+ *                              of consecutive steps is multiplied into a
+ *                              double-float running product (sliced products
+ *                              again on the tensor cores) and the chunk
+ *                              products are combined by a double-float tree
+ *                              (d <= 64) or an FP64 tree (d > 64).
  *                              The Chebyshev order is the smallest odd order
  *                              whose truncation summed over all steps stays
  *                              below 1e-9. */
