@@ -46,6 +46,7 @@ struct Ctx {
     int precision = PARAMENT_PRECISION_PLAIN;
     DevBuf split_stack;                          // split form's stack (commutators from FP64)
     bool split_ready = false;
+    bool split_herm = false;                     // split stack exactly (anti-)Hermitian per slot
 
     // Instrumentation: CUDA events around the dominant kernel of the last call
     // and the number of kernels it launched.

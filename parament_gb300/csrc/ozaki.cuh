@@ -73,12 +73,28 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
         : "memory");
 }
 
+// Where the B slices of a product sit: slice t at sb + t * stride, its K half
+// 0 (rows 0..63 of [B_r; B_i]) at + h0 and K half 1 at + h1, each a 64 x 64
+// block stored K-major ([B^T] rows) or MN-major ([B] rows).
+struct BLayout {
+    uint32_t stride, h0, h1;
+    bool mn;
+};
+// B slices of their own: [B_r][B_i] blocks per slice, MN-major or K-major.
+constexpr BLayout kBSlicesMn = {(uint32_t)kBSlice, 0u, (uint32_t)kBlk, true};
+constexpr BLayout kBSlicesK = {(uint32_t)kBSlice, 0u, (uint32_t)kBlk, false};
+// B = A^H read from the A slices of a Hermitian operand: B^T = conj(A), so
+// the K-major blocks B_r^T = A_r and B_i^T = -A_i are the [A_r] and [-A_i]
+// blocks of A's slices, and A's row scales are B's column scales.
+constexpr BLayout kBFromHermA = {(uint32_t)kASlice, (uint32_t)kBlk, 0u, false};
+
 // Issues the MMAs of one sliced product (one thread).  Slices s < sa_n of A
-// at sa (kASlice bytes each) and t < sb_n of B at sb (kBSlice each, K-major
-// or, with b_mn, MN-major); level L = s + t <= lmax accumulates at tmem
-// column d_tmem + 64 L.  With imag set the product is i * A * B.
+// at sa (kASlice bytes each) and t < sb_n of B at sb (laid out as bl says);
+// level L = s + t <= lmax accumulates at tmem column d_tmem + 64 L.  With
+// imag set the product is i * A * B.
 __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint32_t sb, int sa_n, int sb_n,
-                                              int lmax, bool imag, bool b_mn = false) {
+                                              int lmax, bool imag, BLayout bl = kBSlicesK) {
+    const bool b_mn = bl.mn;
     const uint32_t id_pos = idesc_bf16(false, b_mn), id_neg = idesc_bf16(true, b_mn);
     // B address of K chunk kk (16 K values) within one K half: 32 bytes along
     // a K-major row, or 16 rows of 128 bytes MN-major.
@@ -89,21 +105,21 @@ __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint
             const int L = s + t;
             if (L > lmax) continue;
             const uint32_t d = d_tmem + 64u * (uint32_t)L;
-            const uint32_t a = sa + (uint32_t)s * kASlice, b = sb + (uint32_t)t * kBSlice;
+            const uint32_t a = sa + (uint32_t)s * kASlice, b = sb + (uint32_t)t * bl.stride;
             // K half 0: A' columns 0..63 = [A_r; A_i] (i*A: [-A_i; A_r]), B rows 0..63 = B_r.
             const uint32_t a0 = imag ? a : a + kBlk;
             // K half 1: [-A_i; A_r] (i*A: -[A_r; A_i]), B rows 64..127 = B_i.
             const uint32_t a1 = imag ? a + kBlk : a;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-                const uint32_t bb = b + b_step * kk;
+                const uint32_t bb = b + bl.h0 + b_step * kk;
                 mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), b_mn ? desc_mn_sw128(bb) : tc::desc_k_sw128(bb), id_pos,
                          ((started >> L) & 1u) | (kk > 0 ? 1u : 0u));
             }
             started |= 1u << L;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-                const uint32_t bb = b + kBlk + b_step * kk;
+                const uint32_t bb = b + bl.h1 + b_step * kk;
                 mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), b_mn ? desc_mn_sw128(bb) : tc::desc_k_sw128(bb),
                          imag ? id_neg : id_pos, 1u);
             }

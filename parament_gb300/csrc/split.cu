@@ -23,6 +23,7 @@
 // all P steps (2 P |J_(M+1)(x)|), stays below 1e-9; x = Hnorm * dt_eff must
 // not exceed 0.5 so that the regrouped polynomial has no cancellation.
 #include <math.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <vector>
@@ -532,10 +533,33 @@ static Parament_ErrorCode prepare_split_stack(Ctx *c) {
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     tmp.release();
+    // Exact (anti-)Hermitian symmetry of the complex64 stack: H_0 and H_k
+    // Hermitian, the commutator slots anti-Hermitian.  With real control
+    // weights and imaginary commutator weights every X_j is then exactly
+    // Hermitian, which the tensor-core kernel exploits.
+    bool herm = true;
+    if (e == cudaSuccess) {
+        std::vector<float2> h(n);
+        e = cudaMemcpy(h.data(), c->split_stack.ptr, n * sizeof(float2), cudaMemcpyDeviceToHost);
+        const unsigned d = c->dim;
+        for (size_t m = 0; e == cudaSuccess && herm && m < 1 + (size_t)c->Ke; ++m) {
+            const float sg = m <= K ? 1.0f : -1.0f;  // +: Hermitian, -: anti-Hermitian
+            const float2 *x = h.data() + m * dd;
+            for (unsigned i = 0; herm && i < d; ++i)
+                for (unsigned j = 0; j <= i; ++j) {
+                    const float2 u = x[(size_t)i * d + j], v = x[(size_t)j * d + i];
+                    if (!(u.x == sg * v.x && u.y == -sg * v.y)) {
+                        herm = false;
+                        break;
+                    }
+                }
+        }
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         return PARAMENT_STATUS_CUBLAS_FAILED;
     }
+    c->split_herm = herm;
     c->split_ready = true;
     return PARAMENT_STATUS_SUCCESS;
 }
@@ -566,6 +590,10 @@ Parament_ErrorCode run_split(Ctx *c, const void *d_carr, unsigned pts, unsigned 
     a.magnus = c->magnus ? 1 : 0;
     a.hfac = h / 12.0;
     a.fault = c->d_fault;
+    // PARAMENT_SPLIT_HERMITIAN=0 turns the Hermitian-step shortcut of the
+    // tensor-core kernel off (a test hook: the results are bit-identical).
+    const char *hv = getenv("PARAMENT_SPLIT_HERMITIAN");
+    a.herm_stack = (c->split_herm && !(hv && hv[0] == '0')) ? 1 : 0;
     a.wts = nullptr;
     a.xplanes = nullptr;
     a.chunks = nullptr;

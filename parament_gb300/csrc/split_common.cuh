@@ -95,6 +95,7 @@ struct SplitArgs {
     const float4 *wts;                  // P x Ke step weights in double-float (re hi, re lo, im hi, im lo)
     const float *xplanes;               // X planes of the steps of one launch (tensor-core form)
     int *fault;                         // the context's counter of CTAs whose bounded waits gave up
+    int herm_stack;                     // H_0, H_k exactly Hermitian and the commutators exactly anti-Hermitian
 };
 
 // Weight m of step s in FP64 from complex64 samples (src/cuda/control_expansion.cu:27-170,

@@ -30,11 +30,22 @@
 // forms it for every step) and each thread forms its plane of mu_1 X from the
 // other plane there.
 //
+// When X_j is exactly Hermitian (Hermitian inputs and real control samples;
+// k_split_assemble flags each step), so is the computed X^2 (exact integer
+// level sums, symmetric scales), and the products X X, X^2 X^2 and
+// X^(2k-2) X^2 take their B operand straight from the A slices of X or X^2:
+// B^T = conj(A), the [A_r] and [-A_i] blocks (ozaki.cuh, kBFromHermA), with
+// the row scales as column scales.  The slices are the same numbers the B
+// slicing would produce, so the result is bit-identical; such a step just
+// skips the B slicing of X and X^2 with their column maxima, and forms E from
+// the planes while the tensor core runs X^2.
+//
 // Layout of one CTA (512 threads, one per SM): shared memory holds the A
 // slices (4 x 24 KB), the B slices (4 x 16 KB) and a third buffer (2 x 24 KB)
-// for the A slices of X^4, X^6 and then the B slices of N; at the start of a
-// step the A slice buffer receives the planes that hand X_j to the lane
-// layout.  Tensor memory holds the product levels (columns 0..255), E^P in
+// for the A slices of X^4, X^6 (Hermitian steps: of X^2) and then the B
+// slices of N; at the start of a step the B and third buffers receive the
+// planes that hand X_j to the lane layout (Hermitian steps put the A slices
+// of X^4, X^6 in the B buffer).  Tensor memory holds the product levels (columns 0..255), E^P in
 // double-float (256..383) and E of the current step (384..511) while the
 // polynomial products run.  Sixteen warps hide the latency of the elementwise
 // work (slicing, epilogues) that surrounds each product; each thread owns one
@@ -71,15 +82,24 @@ constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
 // for the odd part X Q and the B buffer is free for E^P while X Q runs.
 constexpr size_t kTcdSG = (size_t)kTcdG * oz::kASlice;
 constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdSG + 1024;
-// X_j reaches the lane layout through four planes (re hi, re lo, im hi, im
+// X_j reaches the lane layout through four planes (re hi, im hi, re lo, im
 // lo) of 64 rows padded to 68 floats (conflict-free 16-byte reads of a column
 // block by 32 consecutive rows).  k_split_assemble writes them for every step
-// in that layout; one bulk copy per step brings them into the A slice buffer,
-// which is free from the end of a step's last product to the X^2 slicing.
+// in that layout.  The hi pair and the lo pair travel by separate bulk copies
+// of kTcdPairBytes each: the hi pair into the third slice buffer, free from
+// the end of a step's X Q product to the next step's X^2 epilogue (a whole
+// step ahead), the lo pair into the B slice buffer, free from the end of the
+// running product to the next step's X^2 slicing.
 constexpr int kTcdPlaneLd = 68;
 constexpr int kTcdPlane = 64 * kTcdPlaneLd;
-constexpr uint32_t kTcdXBytes = 4 * kTcdPlane * sizeof(float);
-static_assert(kTcdXBytes <= kTcdSA && kTcdXBytes % 16 == 0, "planes exceed the A slice buffer");
+constexpr uint32_t kTcdPairBytes = 2 * kTcdPlane * sizeof(float);
+static_assert(kTcdPairBytes <= kTcdSG && kTcdPairBytes <= kTcdSB && kTcdPairBytes % 16 == 0,
+              "plane pairs exceed their slice buffers");
+// Float index, within the planes of a step, of the flag that k_split_assemble
+// leaves in the row padding (plane 0, row 0, column 64): nonzero when X_j is
+// exactly Hermitian (Hermitian inputs, anti-Hermitian commutators, real
+// control weights and imaginary commutator weights).
+constexpr int kTcdHermFlag = 64;
 static_assert(kTcdPlane * 4 == kSplitXStride, "plane layout of k_split_assemble");
 
 // Bounded waits that gave up, for launches without a context's counter.
@@ -138,7 +158,7 @@ struct TcdShared {
     float rowmul_x[64];            // the same for the A slices of X (X^2 and X Q)
     float colmul_p[64];            // column scales of the running product's B (E^P)
     uint64_t bar;                  // tensor-core products
-    uint64_t tbar;                 // bulk copies of the X planes
+    uint64_t hbar, lbar;           // bulk copies of the X planes (hi pair, lo pair)
     uint32_t tmem_base;
 };
 
@@ -189,11 +209,16 @@ __device__ __forceinline__ float unscale_of(int mbits) {
     return __int_as_float((max(mbits, 27 << 23) & 0x7F800000) - (6 << 23));
 }
 
-template <int S, bool DF>
+// With SETCOL the row scales also become the column scales (colmul): the
+// product's B is this A's conjugate transpose, read from the same slices.
+template <int S, bool DF, bool SETCOL = false>
 __device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const TcdThread &t, int b,
                                         const float (&hi)[16], const float (&lo)[16]) {
     const int mb = sh.amax[b][t.r];
-    if (t.p == 0 && t.cb == 0) sh.rowmul[t.r] = unscale_of(mb);
+    if (t.p == 0 && t.cb == 0) {
+        sh.rowmul[t.r] = unscale_of(mb);
+        if (SETCOL) sh.colmul[t.r] = unscale_of(mb);
+    }
     const float sc = scale_of(mb);
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
@@ -215,12 +240,14 @@ __device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const 
 
 // B slices, MN-major: row r of plane p is K row 64 p + r of [B_r; B_i], the
 // thread's 16 columns are contiguous within it.
+// `cmax` holds the column maxima (float bits): sh.bmax of the product, or,
+// for a Hermitian B, sh.amax (its row maxima, the same numbers).
 template <int S, bool DF>
-__device__ __forceinline__ void store_b(TcdShared &sh, unsigned char *SB, const TcdThread &t, int b,
+__device__ __forceinline__ void store_b(unsigned char *SB, const TcdThread &t, const int *cmax,
                                         const float (&hi)[16], const float (&lo)[16], float *colmul) {
-    if (t.p == 0 && t.r < 16) colmul[t.c0 + t.lane] = unscale_of(sh.bmax[b][t.c0 + t.lane]);
+    if (t.p == 0 && t.r < 16) colmul[t.c0 + t.lane] = unscale_of(cmax[t.c0 + t.lane]);
     const int k = 64 * t.p + t.r;
-    const int4 *cm = reinterpret_cast<const int4 *>(sh.bmax[b] + t.c0);
+    const int4 *cm = reinterpret_cast<const int4 *>(cmax + t.c0);
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
         const int4 m0 = cm[2 * g], m1 = cm[2 * g + 1];
@@ -248,14 +275,15 @@ __device__ __forceinline__ void store_b(TcdShared &sh, unsigned char *SB, const 
 // the issue combines it over the CTA, and a product is issued only if every
 // earlier wait succeeded (returns false otherwise, in every thread).
 __device__ __forceinline__ bool issue_sliced(TcdShared &sh, const TcdThread &t, unsigned char *SA, unsigned char *SB,
-                                             int sa_n, int sb_n, int lmax, bool imag, bool ok) {
+                                             int sa_n, int sb_n, int lmax, bool imag, bool ok,
+                                             oz::BLayout bl = oz::kBSlicesMn) {
     tc::fence_proxy_async();
     tc::fence_before_sync();
     const bool all_ok = __syncthreads_and(ok) != 0;
     tc::fence_after_sync();
     if (!all_ok) return false;
     if (t.tid == 0) {
-        oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, true);
+        oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, bl);
         tc::mma_commit(&sh.bar);
     }
     return true;
@@ -267,8 +295,9 @@ __device__ __forceinline__ void wait_sliced(TcdShared &sh, uint32_t &ncommit, bo
     tc::fence_after_sync();
 }
 __device__ __forceinline__ bool run_product(TcdShared &sh, const TcdThread &t, unsigned char *SA, unsigned char *SB,
-                                            int sa_n, int sb_n, int lmax, bool imag, uint32_t &ncommit, bool &ok) {
-    if (!issue_sliced(sh, t, SA, SB, sa_n, sb_n, lmax, imag, ok)) return false;
+                                            int sa_n, int sb_n, int lmax, bool imag, uint32_t &ncommit, bool &ok,
+                                            oz::BLayout bl = oz::kBSlicesMn) {
+    if (!issue_sliced(sh, t, SA, SB, sa_n, sb_n, lmax, imag, ok, bl)) return false;
     wait_sliced(sh, ncommit, ok);
     return true;
 }
@@ -447,7 +476,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     }
     if (t.tid == 0) {
         tc::mbar_init(&sh.bar, 1);
-        tc::mbar_init(&sh.tbar, 1);
+        tc::mbar_init(&sh.hbar, 1);
+        tc::mbar_init(&sh.lbar, 1);
         tc::fence_mbar_init();
     }
     if (t.tid < 64) {
@@ -470,59 +500,95 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
     uint32_t ncommit = 0;
     int nb = 0;  // max-buffer parity
     bool ok = true;
-    // The X planes of step st reach the A slice buffer by one bulk copy, issued
-    // as soon as the previous step's last product is done with the buffer.
-    uint32_t tphase = 0, tissued = 0;  // copies waited for / issued (same in every thread)
-    auto issue_x = [&](long long st) {
-        ++tissued;
+    // The X planes of step st reach shared memory by two bulk copies: the hi
+    // pair (what a step reads first) into the third slice buffer SG as soon as
+    // the previous step's X Q product is done with it, the lo pair into the B
+    // slice buffer SB once the previous step's running product is.
+    uint32_t hphase = 0, hissued = 0, lphase = 0, lissued = 0;  // copies waited for / issued (same in every thread)
+    auto issue_hi = [&](long long st) {
+        ++hissued;
         if (t.tid == 0) {
-            mbar_expect_tx(&sh.tbar, kTcdXBytes);
-            bulk_g2s(SA, a.xplanes + (size_t)st * kSplitXStride, kTcdXBytes, &sh.tbar);
+            mbar_expect_tx(&sh.hbar, kTcdPairBytes);
+            bulk_g2s(SG, a.xplanes + (size_t)st * kSplitXStride, kTcdPairBytes, &sh.hbar);
         }
     };
-    if (s1 > s0) issue_x(s0);
+    auto issue_lo = [&](long long st) {
+        ++lissued;
+        if (t.tid == 0) {
+            mbar_expect_tx(&sh.lbar, kTcdPairBytes);
+            bulk_g2s(SB, a.xplanes + (size_t)st * kSplitXStride + 2 * kTcdPlane, kTcdPairBytes, &sh.lbar);
+        }
+    };
+    const float *XH = reinterpret_cast<const float *>(SG);
+    const float *XL = reinterpret_cast<const float *>(SB);
+    // E = c0 I + i nu_1 X in this thread's plane (E_re = c0 d - nu_1 X_im,
+    // E_im = nu_1 X_re), from the other plane's double-float X; E waits in
+    // tensor memory while the polynomial products run.
+    auto form_e = [&]() {
+        ok = tc::mbar_wait(&sh.lbar, lphase & 1, kTcdWait) && ok;
+        ++lphase;
+        float Eh[16], El[16];
+        const float4 *oh = reinterpret_cast<const float4 *>(XH + (1 - t.p) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
+        const float4 *ol = reinterpret_cast<const float4 *>(XL + (1 - t.p) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const float4 h = oh[g], l = ol[g];
+            const float hs[4] = {h.x, h.y, h.z, h.w}, ls[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int j = 4 * g + i;
+                df e = df_mul(nu1, df{hs[i], ls[i]});
+                if (t.p == 0) {
+                    e = df_neg(e);
+                    if (t.c0 + j == t.r) e = df_add(e, c0d);
+                }
+                Eh[j] = e.hi;
+                El[j] = e.lo;
+            }
+        }
+        store_ep(t.tm_e, Eh, El);
+    };
+    if (s1 > s0) {
+        issue_hi(s0);
+        issue_lo(s0);
+    }
     for (long long st = s0; st < s1; ++st) {
+        ok = tc::mbar_wait(&sh.hbar, hphase & 1, kTcdWait) && ok;
+        ++hphase;
+        // Hermitian step (flag in the planes' row padding, k_split_assemble):
+        // the products of X and X^2 take their B operands from the A slices,
+        // and E is formed while the tensor core runs X^2.
+        const bool herm = XH[kTcdHermFlag] != 0.0f;
         float X[16];
         {
-            ok = tc::mbar_wait(&sh.tbar, tphase & 1, kTcdWait) && ok;
-            ++tphase;
-            const float *XP = reinterpret_cast<const float *>(SA);
-            // E = c0 I + i nu_1 X in this thread's plane: E_re = c0 d - nu_1 X_im,
-            // E_im = nu_1 X_re.
-            {
-                float Eh[16], El[16];
-                const float4 *own = reinterpret_cast<const float4 *>(XP + 2 * t.p * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
-                const float4 *oh = reinterpret_cast<const float4 *>(XP + 2 * (1 - t.p) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
-                const float4 *ol = reinterpret_cast<const float4 *>(XP + (2 * (1 - t.p) + 1) * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
+            const float4 *own = reinterpret_cast<const float4 *>(XH + t.p * kTcdPlane + t.r * kTcdPlaneLd + t.c0);
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
-                    const float4 x = own[g], h = oh[g], l = ol[g];
-                    const float xs[4] = {x.x, x.y, x.z, x.w}, hs[4] = {h.x, h.y, h.z, h.w}, ls[4] = {l.x, l.y, l.z, l.w};
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const int j = 4 * g + i;
-                        X[j] = xs[i];
-                        df e = df_mul(nu1, df{hs[i], ls[i]});
-                        if (t.p == 0) {
-                            e = df_neg(e);
-                            if (t.c0 + j == t.r) e = df_add(e, c0d);
-                        }
-                        Eh[j] = e.hi;
-                        El[j] = e.lo;
-                    }
-                }
-                // E waits in tensor memory while the polynomial products run.
-                store_ep(t.tm_e, Eh, El);
+            for (int g = 0; g < 4; ++g) {
+                const float4 x = own[g];
+                X[4 * g] = x.x;
+                X[4 * g + 1] = x.y;
+                X[4 * g + 2] = x.z;
+                X[4 * g + 3] = x.w;
             }
         }
         // ---- X^2
-        float N[16], G[16];
-        reduce_max<true, true>(sh, t, nb, X, X);
-        store_a<kTcdX2, false>(sh, SA, t, nb, X, X);
-        store_b<kTcdX2, false>(sh, SB, t, nb, X, X, sh.colmul);
-        nb ^= 1;
-        if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit, ok)) break;
+        if (herm) {
+            reduce_max<true, false>(sh, t, nb, X, X);
+            store_a<kTcdX2, false, true>(sh, SA, t, nb, X, X);
+            nb ^= 1;
+            if (!issue_sliced(sh, t, SA, SA, kTcdX2, kTcdX2, kTcdX2 - 1, false, ok, oz::kBFromHermA)) break;
+            form_e();
+            wait_sliced(sh, ncommit, ok);
+        } else {
+            form_e();  // before the B slices of X overwrite the planes
+            reduce_max<true, true>(sh, t, nb, X, X);
+            store_a<kTcdX2, false>(sh, SA, t, nb, X, X);
+            store_b<kTcdX2, false>(SB, t, sh.bmax[nb], X, X, sh.colmul);
+            nb ^= 1;
+            if (!run_product(sh, t, SA, SB, kTcdX2, kTcdX2, kTcdX2 - 1, false, ncommit, ok)) break;
+        }
         if (t.tid < 64) sh.rowmul_x[t.tid] = sh.rowmul[t.tid];
+        float N[16], G[16];
         epilogue_f<kTcdX2 - 1>(sh, t, G);
         {
             const float nu3 = (float)a.mu[3].y;
@@ -539,20 +605,35 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         }
         // ---- higher even powers X^(2k) = X^(2k-2) X^2.  Their terms mu_(2k) X^(2k)
         // are of order (h ||X||)^4 and below: they collect in FP32 (Se) and
-        // reach E together with the odd part.
+        // reach E together with the odd part.  Hermitian steps keep the A
+        // slices of X^2 in SG (they are also the B operand of every X^(2k)
+        // product) and put those of X^(2k-2), k > 2, in SB.
         float Se[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) Se[j] = 0.0f;
         bool live = true;
         for (int k = 2; 2 * k <= M; ++k) {
-            if (k == 2)
-                reduce_max<true, true>(sh, t, nb, G, G);
-            else
+            if (herm) {
                 reduce_max<true, false>(sh, t, nb, G, G);
-            store_a<kTcdG, false>(sh, SG, t, nb, G, G);
-            if (k == 2) store_b<kTcdG, false>(sh, SB, t, nb, G, G, sh.colmul);
-            nb ^= 1;
-            if (!(live = run_product(sh, t, SG, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok))) break;
+                unsigned char *dst = k == 2 ? SG : SB;
+                if (k == 2)
+                    store_a<kTcdG, false, true>(sh, dst, t, nb, G, G);
+                else
+                    store_a<kTcdG, false>(sh, dst, t, nb, G, G);
+                nb ^= 1;
+                if (!(live = run_product(sh, t, dst, SG, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok,
+                                         oz::kBFromHermA)))
+                    break;
+            } else {
+                if (k == 2)
+                    reduce_max<true, true>(sh, t, nb, G, G);
+                else
+                    reduce_max<true, false>(sh, t, nb, G, G);
+                store_a<kTcdG, false>(sh, SG, t, nb, G, G);
+                if (k == 2) store_b<kTcdG, false>(SB, t, sh.bmax[nb], G, G, sh.colmul);
+                nb ^= 1;
+                if (!(live = run_product(sh, t, SG, SB, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok))) break;
+            }
             epilogue_f<kTcdG - 1>(sh, t, G);
             const float me = (float)a.mu[2 * k].x;
             const float no = (2 * k + 1 <= M) ? (float)a.mu[2 * k + 1].y : 0.0f;
@@ -564,10 +645,12 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         }
         if (!live) break;
         // ---- odd part X Q = i X N: the A slices of X are still in SA; the B
-        // slices of N go to SG (free after X^6).
+        // slices of N go to SG (free after the last even power).  N is sliced
+        // with its own column maxima on every step: X^6 = X^4 X^2 from
+        // truncated slices is Hermitian only to their precision, and so is N.
         reduce_max<false, true>(sh, t, nb, X, N);
         if (t.tid < 64) sh.rowmul[t.tid] = sh.rowmul_x[t.tid];
-        store_b<kTcdX2, false>(sh, SG, t, nb, N, N, sh.colmul);
+        store_b<kTcdX2, false>(SG, t, sh.bmax[nb], N, N, sh.colmul);
         nb ^= 1;
         if (!issue_sliced(sh, t, SA, SG, kTcdX2, kTcdX2, kTcdX2 - 1, true, ok)) break;
         if (st > s0) {
@@ -577,9 +660,10 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
             float Ph[16], Pl[16];
             load_ep(t.tm_ep, Ph, Pl);
             reduce_max<false, true>(sh, t, nb, Ph, Ph);
-            store_b<kTcdHi, true>(sh, SB, t, nb, Ph, Pl, sh.colmul_p);
+            store_b<kTcdHi, true>(SB, t, sh.bmax[nb], Ph, Pl, sh.colmul_p);
         }
         wait_sliced(sh, ncommit, ok);
+        if (st + 1 < s1) issue_hi(st + 1);  // SG is free again
         epilogue_f<kTcdX2 - 1>(sh, t, G);
         float Eh[16], El[16];
         load_ep(t.tm_e, Eh, El);
@@ -591,14 +675,14 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         }
         // ---- running product E^P <- E^P + E + E E^P
         if (st == s0) {
-            if (st + 1 < s1) issue_x(st + 1);  // the slice buffers are free again
+            if (st + 1 < s1) issue_lo(st + 1);  // SB is free again
             store_ep(t.tm_ep, Eh, El);
         } else {
             reduce_max<true, false>(sh, t, nb, Eh, Eh);
             store_a<kTcdHi, true>(sh, SA, t, nb, Eh, El);
             nb ^= 1;
             if (!run_product(sh, t, SA, SB, kTcdHi, kTcdHi, kTcdHi - 1, false, ncommit, ok)) break;
-            if (st + 1 < s1) issue_x(st + 1);  // the slice buffers are free again
+            if (st + 1 < s1) issue_lo(st + 1);  // SB is free again
             epilogue_running(sh, t, Eh, El);
         }
     }
@@ -623,7 +707,8 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         // and shared memory are released.
         if (ncommit > 0) tc::mbar_wait(&sh.bar, (ncommit - 1) & 1, kTcdWait);
     }
-    for (; tphase < tissued; ++tphase) tc::mbar_wait(&sh.tbar, tphase & 1, kTcdWait);
+    for (; hphase < hissued; ++hphase) tc::mbar_wait(&sh.hbar, hphase & 1, kTcdWait);
+    for (; lphase < lissued; ++lphase) tc::mbar_wait(&sh.lbar, lphase & 1, kTcdWait);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
@@ -642,7 +727,7 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
 // element takes the same operations in the same order as an assembly inside
 // the step kernel would (real weights: paired double-float multiply-add;
 // complex weights: complex double-float; commutator slots: FP32 sums added at
-// the end).  Output: four planes (re hi, re lo, im hi, im lo) of 64 rows x 68
+// the end).  Output: four planes (re hi, im hi, re lo, im lo) of 64 rows x 68
 // floats per step, kSplitXStride floats apart.
 constexpr int kAsmSteps = 32;
 // Shared memory of k_split_assemble at the largest Ke: its stack slice and the
@@ -723,15 +808,26 @@ __global__ void __launch_bounds__(128) k_split_assemble(const __grid_constant__ 
         const df i1 = df_add_f(df_norm(xih[1], xil[1]), si[1]);
         float *o = xp + (size_t)s * kSplitXStride + row * kTcdPlaneLd + col;
         *reinterpret_cast<float2 *>(o) = make_float2(r0.hi, r1.hi);
-        *reinterpret_cast<float2 *>(o + kTcdPlane) = make_float2(r0.lo, r1.lo);
-        *reinterpret_cast<float2 *>(o + 2 * kTcdPlane) = make_float2(i0.hi, i1.hi);
+        *reinterpret_cast<float2 *>(o + kTcdPlane) = make_float2(i0.hi, i1.hi);
+        *reinterpret_cast<float2 *>(o + 2 * kTcdPlane) = make_float2(r0.lo, r1.lo);
         *reinterpret_cast<float2 *>(o + 3 * kTcdPlane) = make_float2(i0.lo, i1.lo);
         if (col == 62) {
             // The row padding too, so that every 32-byte sector of the planes
-            // is written whole (no read of a partly written sector).
+            // is written whole (no read of a partly written sector); row 0 of
+            // plane 0 carries the step's Hermitian flag.
+            float flag = 0.0f;
+            if (row == 0 && a.herm_stack) {
+                bool herm = true;
+                for (int m = 0; m < Ke; ++m) {
+                    const float4 w = ws[m];
+                    herm = herm && (m < a.K ? (w.z == 0.0f && w.w == 0.0f) : (w.x == 0.0f && w.y == 0.0f));
+                }
+                flag = herm ? 1.0f : 0.0f;
+            }
 #pragma unroll
             for (int pl = 0; pl < 4; ++pl)
-                *reinterpret_cast<float4 *>(o + pl * kTcdPlane + 2) = make_float4(0.f, 0.f, 0.f, 0.f);
+                *reinterpret_cast<float4 *>(o + pl * kTcdPlane + 2) =
+                    make_float4(pl == 0 ? flag : 0.f, 0.f, 0.f, 0.f);
         }
     }
 }

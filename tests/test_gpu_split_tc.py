@@ -153,3 +153,54 @@ def test_wide_expansion_magnus_k5(built_lib):
     U, _ = split_equiprop(H0, H1, list(carr), 1e-3, True, oracle.SIMPSON)
     Uo = oracle.equiprop(H0, H1, carr, 1e-3, magnus=True, mode=oracle.SIMPSON, nthreads=os.cpu_count())[0]
     assert relerr(U, Uo) < TOL
+
+
+@pytest.mark.parametrize("dt,magnus,order,n,seed", [(1e-3, True, 7, 2 * 1024 + 1, 17), (1.6e-2, False, 9, 257, 5)])
+def test_hermitian_steps_bit_identical(built_lib, dt, magnus, order, n, seed):
+    """Hermitian inputs with real samples take the kernel's Hermitian-step
+    shortcut (the B operands of X X, X^2 X^2 and X^(2k-2) X^2 read from the A
+    slices).  Those slices are the numbers the B slicing would produce, so the
+    propagator is bit-identical to the general path's (shortcut switched off
+    with PARAMENT_SPLIT_HERMITIAN=0); order 9 also covers X^8 = X^6 X^2."""
+    K = 4 if magnus else 2
+    H0, H1, carr = problem(K, n, seed=seed, norm0=5.0 if order == 9 else 10.0)
+    mode = oracle.SIMPSON if magnus else oracle.NONE
+    U1, M = split_equiprop(H0, H1, list(carr), dt, magnus, mode)
+    old = os.environ.get("PARAMENT_SPLIT_HERMITIAN")
+    os.environ["PARAMENT_SPLIT_HERMITIAN"] = "0"
+    try:
+        U0, _ = split_equiprop(H0, H1, list(carr), dt, magnus, mode)
+    finally:
+        if old is None:
+            del os.environ["PARAMENT_SPLIT_HERMITIAN"]
+        else:
+            os.environ["PARAMENT_SPLIT_HERMITIAN"] = old
+    assert M == order
+    assert np.array_equal(U1, U0)
+    Uo = oracle.equiprop(H0, H1, carr, dt, magnus=magnus, mode=mode, nthreads=os.cpu_count())[0]
+    assert relerr(U1, Uo) < TOL
+
+
+def test_non_hermitian_hamiltonian(built_lib):
+    """A drift with a small anti-Hermitian part (a lossy system): no step is
+    Hermitian, every product slices its B operand.  Against the FP64 oracle."""
+    from parament_gb300.workloads import hermitian
+    H0, H1, carr = problem(3, 2 * 500 + 1, seed=23)
+    H0 = c64(H0 + 0.05j * hermitian(np.random.default_rng(24), 64, 1.0))
+    U, _ = split_equiprop(H0, H1, list(carr), 1e-3, True, oracle.SIMPSON)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, magnus=True, mode=oracle.SIMPSON, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
+
+
+def test_hermitian_and_general_steps_mixed(built_lib):
+    """Samples with imaginary parts on a few stretches only: steps touching
+    them take the general path, the others the Hermitian one, within one
+    chunk.  Against the FP64 oracle."""
+    H0, H1, carr = problem(3, 2 * 3000 + 1, seed=29)
+    rng = np.random.default_rng(30)
+    for lo in (100, 2000, 4500):
+        carr[:, lo:lo + 37] += 1j * rng.standard_normal((3, 37))
+    carr = c64(carr)
+    U, _ = split_equiprop(H0, H1, list(carr), 1e-3, True, oracle.SIMPSON)
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, magnus=True, mode=oracle.SIMPSON, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
