@@ -44,19 +44,21 @@ __device__ __forceinline__ uint32_t sw(int row, int k) {
 }
 
 // kind::f16 instruction descriptor: BF16 x BF16 -> FP32, A K-major, M = 128,
-// N = 64; bit 13 negates A, bit 16 selects an MN-major B.
-__host__ __device__ constexpr uint32_t idesc_bf16(bool negate_a, bool b_mn = false) {
+// N columns (a multiple of 16 up to 256); bit 13 negates A, bit 16 selects an
+// MN-major B.
+__host__ __device__ constexpr uint32_t idesc_bf16(bool negate_a, bool b_mn = false, int N = 64) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((negate_a ? 1u : 0u) << 13) | ((b_mn ? 1u : 0u) << 16) |
-           ((uint32_t)(64 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
 
-// Shared-memory descriptor of an MN-major operand with the 128-byte swizzle
-// and 64 bf16 per row: one swizzle atom across N, 1024 bytes between groups of
-// eight K rows.
-__device__ __forceinline__ uint64_t desc_mn_sw128(uint32_t saddr) {
+// Shared-memory descriptor of an MN-major operand with the 128-byte swizzle:
+// 64 bf16 of N per swizzle atom, 1024 bytes between groups of eight K rows
+// (stride byte offset), and `atom_stride` bytes from one atom of 64 N columns
+// to the next (leading byte offset; unused when N = 64).
+__device__ __forceinline__ uint64_t desc_mn_sw128(uint32_t saddr, uint32_t atom_stride = 16u) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)((atom_stride >> 4) & 0x3FFF) << 16;
     d |= (uint64_t)(1024 >> 4) << 32;
     d |= (uint64_t)1 << 46;
     d |= (uint64_t)2 << 61;
@@ -124,6 +126,40 @@ __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint
                          imag ? id_neg : id_pos, 1u);
             }
         }
+    }
+}
+
+// The same product with MN-major B slices (kBSlice apart) stacked along N: for
+// A slice s one chain of MMAs with N = 64 n_t covers B slices t = 0 .. n_t - 1,
+// n_t = min(sb_n, lmax - s + 1), and writes levels s .. s + n_t - 1 at their
+// tensor-memory columns d_tmem + 64 (s + t), which are contiguous.  A is read
+// once per A slice instead of once per slice pair: the N = 64 products are
+// bound by the shared-memory operand reads (6 KB per MMA).  With lmax < sb_n
+// slice s = 0 covers every level and starts them (first MMA without
+// accumulate), so the sums and their order per level are those of
+// issue_product; other shapes go to issue_product.
+__device__ __forceinline__ void issue_product_stacked(uint32_t d_tmem, uint32_t sa, uint32_t sb, int sa_n, int sb_n,
+                                                      int lmax, bool imag) {
+    if (lmax >= sb_n) {
+        issue_product(d_tmem, sa, sb, sa_n, sb_n, lmax, imag, kBSlicesMn);
+        return;
+    }
+    for (int s = 0; s < sa_n; ++s) {
+        const int nt = min(sb_n, lmax - s + 1);
+        if (nt <= 0) continue;
+        const uint32_t id_pos = idesc_bf16(false, true, 64 * nt), id_neg = idesc_bf16(true, true, 64 * nt);
+        const uint32_t d = d_tmem + 64u * (uint32_t)s;
+        const uint32_t a = sa + (uint32_t)s * kASlice;
+        const uint32_t a0 = imag ? a : a + kBlk;
+        const uint32_t a1 = imag ? a + kBlk : a;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+            mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), desc_mn_sw128(sb + 2048u * kk, (uint32_t)kBSlice), id_pos,
+                     (s > 0 || kk > 0) ? 1u : 0u);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+            mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), desc_mn_sw128(sb + kBlk + 2048u * kk, (uint32_t)kBSlice),
+                     imag ? id_neg : id_pos, 1u);
     }
 }
 

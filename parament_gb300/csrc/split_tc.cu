@@ -283,7 +283,10 @@ __device__ __forceinline__ bool issue_sliced(TcdShared &sh, const TcdThread &t, 
     tc::fence_after_sync();
     if (!all_ok) return false;
     if (t.tid == 0) {
-        oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, bl);
+        if (bl.mn)
+            oz::issue_product_stacked(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag);
+        else
+            oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, bl);
         tc::mma_commit(&sh.bar);
     }
     return true;
