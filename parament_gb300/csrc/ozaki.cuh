@@ -130,36 +130,41 @@ __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint
 }
 
 // The same product with MN-major B slices (kBSlice apart) stacked along N: for
-// A slice s one chain of MMAs with N = 64 n_t covers B slices t = 0 .. n_t - 1,
-// n_t = min(sb_n, lmax - s + 1), and writes levels s .. s + n_t - 1 at their
-// tensor-memory columns d_tmem + 64 (s + t), which are contiguous.  A is read
-// once per A slice instead of once per slice pair: the N = 64 products are
-// bound by the shared-memory operand reads (6 KB per MMA).  With lmax < sb_n
-// slice s = 0 covers every level and starts them (first MMA without
-// accumulate), so the sums and their order per level are those of
-// issue_product; other shapes go to issue_product.
+// A slice s, chains of MMAs with N = 64 n (n <= 4 B slices, N <= 256) cover
+// B slices t = 0 .. n_t - 1, n_t = min(sb_n, lmax - s + 1), and write levels
+// s + t at their tensor-memory columns d_tmem + 64 (s + t), which are
+// contiguous.  A is read once per chain instead of once per slice pair: the
+// N = 64 products are bound by the shared-memory operand reads (6 KB per
+// MMA).  With lmax < sb_n the chains of slice s = 0 cover every level; with
+// `fresh` they start them (first MMA of each without accumulate), otherwise
+// they add to what the levels hold.  Per level the sums are those of
+// issue_product, in the same order; other shapes go to issue_product.
 __device__ __forceinline__ void issue_product_stacked(uint32_t d_tmem, uint32_t sa, uint32_t sb, int sa_n, int sb_n,
-                                                      int lmax, bool imag) {
-    if (lmax >= sb_n) {
+                                                      int lmax, bool imag, bool fresh = true) {
+    if (lmax >= sb_n && fresh) {
         issue_product(d_tmem, sa, sb, sa_n, sb_n, lmax, imag, kBSlicesMn);
         return;
     }
     for (int s = 0; s < sa_n; ++s) {
         const int nt = min(sb_n, lmax - s + 1);
-        if (nt <= 0) continue;
-        const uint32_t id_pos = idesc_bf16(false, true, 64 * nt), id_neg = idesc_bf16(true, true, 64 * nt);
-        const uint32_t d = d_tmem + 64u * (uint32_t)s;
         const uint32_t a = sa + (uint32_t)s * kASlice;
         const uint32_t a0 = imag ? a : a + kBlk;
         const uint32_t a1 = imag ? a + kBlk : a;
+        for (int t0 = 0; t0 < nt; t0 += 4) {
+            const int n = min(4, nt - t0);
+            const uint32_t id_pos = idesc_bf16(false, true, 64 * n), id_neg = idesc_bf16(true, true, 64 * n);
+            const uint32_t d = d_tmem + 64u * (uint32_t)(s + t0);
+            const uint32_t b = sb + (uint32_t)t0 * kBSlice;
+            const uint32_t first = (s == 0 && fresh) ? 0u : 1u;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), desc_mn_sw128(sb + 2048u * kk, (uint32_t)kBSlice), id_pos,
-                     (s > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < 4; ++kk)
+                mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), desc_mn_sw128(b + 2048u * kk, (uint32_t)kBSlice), id_pos,
+                         kk > 0 ? 1u : first);
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), desc_mn_sw128(sb + kBlk + 2048u * kk, (uint32_t)kBSlice),
-                     imag ? id_neg : id_pos, 1u);
+            for (int kk = 0; kk < 4; ++kk)
+                mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), desc_mn_sw128(b + kBlk + 2048u * kk, (uint32_t)kBSlice),
+                         imag ? id_neg : id_pos, 1u);
+        }
     }
 }
 

@@ -34,9 +34,10 @@
 //
 // One CTA of 512 threads per SM walks the (item, block row, block column)
 // units; per K block every thread loads 8 complex values of A and of B (one
-// row, 8 columns), slices them into shared memory, and one thread
-// issues the 120 MMAs (15 slice products of 8 MMAs); the next K block's values
-// are loaded while those run.  Every wait on the tensor core is bounded.
+// row, 8 columns), slices them into shared memory, and one thread issues the
+// 15 slice products as 6 chains of 8 MMAs (the B slices of one A slice stacked
+// along N, ozaki.cuh); the next K block's values are loaded while those run.
+// Every wait on the tensor core is bounded.
 #include <stdlib.h>
 
 #include <algorithm>
@@ -182,7 +183,6 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_cgemm(const __grid_constan
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tm = tmem_base + ((uint32_t)(32 * q4) << 16) + (uint32_t)c0;
-    const uint32_t id = oz::idesc_bf16(false, true);
 
     bool ok = true;
     uint32_t ncommit = 0;
@@ -236,25 +236,10 @@ __global__ void __launch_bounds__(kOzThreads, 1) k_oz_cgemm(const __grid_constan
             __syncthreads();
             tc::fence_after_sync();
             if (tid == 0) {
-                const uint32_t sa0 = tc::smem_addr(SA), sb0 = tc::smem_addr(SB);
-#pragma unroll 1
-                for (int s = 0; s < kOzSlices; ++s)
-#pragma unroll 1
-                    for (int t2 = 0; t2 + s < kOzSlices; ++t2) {
-                        const int L = s + t2;
-                        const uint32_t dt = tmem_base + 64u * (uint32_t)L;
-                        const uint32_t a = sa0 + (uint32_t)s * oz::kASlice, bb = sb0 + (uint32_t)t2 * oz::kBSlice;
-                        // Level L is first written by (s, t2) = (0, L) in the first K block.
-                        const uint32_t fresh = (kb == 0 && s == 0) ? 1u : 0u;
-#pragma unroll
-                        for (int kk = 0; kk < 4; ++kk)
-                            oz::mma_bf16(dt, tc::desc_k_sw128(a + oz::kBlk + 32u * kk), oz::desc_mn_sw128(bb + 2048u * kk),
-                                         id, (fresh && kk == 0) ? 0u : 1u);
-#pragma unroll
-                        for (int kk = 0; kk < 4; ++kk)
-                            oz::mma_bf16(dt, tc::desc_k_sw128(a + 32u * kk),
-                                         oz::desc_mn_sw128(bb + oz::kBlk + 2048u * kk), id, 1u);
-                    }
+                // Levels s + t <= 4, the B slices of each A slice stacked along
+                // N; the first K block starts every level.
+                oz::issue_product_stacked(tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), kOzSlices, kOzSlices,
+                                          kOzSlices - 1, false, kb == 0);
                 tc::mma_commit(&bar);
             }
             // The next K block's values load while the tensor core runs.
