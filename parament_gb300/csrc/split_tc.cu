@@ -405,6 +405,20 @@ __device__ __forceinline__ void store_ep(uint32_t taddr, const float (&hi)[16], 
     tc::tmem_wait_st();
 }
 
+// (c_r, c_i) += w (h_r, h_i) with one paired FMA (each half rounds as fmaf).
+__device__ __forceinline__ void fma2(float &cr, float &ci, float w, float hr, float hi) {
+    asm("{\n\t"
+        ".reg .b64 C, W, H;\n\t"
+        "mov.b64 C, {%0, %1};\n\t"
+        "mov.b64 W, {%2, %2};\n\t"
+        "mov.b64 H, {%3, %4};\n\t"
+        "fma.rn.f32x2 C, W, H, C;\n\t"
+        "mov.b64 {%0, %1}, C;\n\t"
+        "}"
+        : "+f"(cr), "+f"(ci)
+        : "f"(w), "f"(hr), "f"(hi));
+}
+
 // acc += w h for a double-float real w and a float h; the compensation term
 // collects the rounding of the sum and the product without renormalising.
 __device__ __forceinline__ void df_mac_lazy(float &hi, float &lo, float wh, float wl, float h) {
@@ -756,7 +770,18 @@ __global__ void __launch_bounds__(128) k_split_assemble(const __grid_constant__ 
     } else {
         for (int m = 0; m <= Ke; ++m) hs[m * 128 + threadIdx.x] = stack4[(size_t)m * 2048 + f];
     }
-    for (int i = threadIdx.x; i < ns * Ke; i += 128) wsa[i] = a.wts[(size_t)(s_off + sb) * Ke + i];
+    // Per step: does any weight leave the usual pattern (real control
+    // weights, imaginary commutator weights)?  Steps that keep it take the
+    // branch-free loops below.
+    __shared__ int odd_step[kAsmSteps];
+    if (threadIdx.x < kAsmSteps) odd_step[threadIdx.x] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < ns * Ke; i += 128) {
+        const float4 w = a.wts[(size_t)(s_off + sb) * Ke + i];
+        wsa[i] = w;
+        const int m = i % Ke;
+        if (m < a.K ? (w.z != 0.0f || w.w != 0.0f) : (w.x != 0.0f || w.y != 0.0f)) odd_step[i / Ke] = 1;
+    }
     __syncthreads();
     const int row = f >> 5, col = 2 * (f & 31);
     for (int k = 0; k < ns; ++k) {
@@ -766,6 +791,36 @@ __global__ void __launch_bounds__(128) k_split_assemble(const __grid_constant__ 
         if constexpr (RK > 0) h0 = hr[0]; else h0 = hs[threadIdx.x];
         float xrh[2] = {h0.x, h0.z}, xih[2] = {h0.y, h0.w};
         float xrl[2] = {0.f, 0.f}, xil[2] = {0.f, 0.f}, sr[2] = {0.f, 0.f}, si[2] = {0.f, 0.f};
+        if (!odd_step[k]) {
+            // Real control weights: paired double-float multiply-adds.
+#pragma unroll
+            for (int m = 0; m < (RK > 0 ? RK : 1 << 30); ++m) {
+                if (m >= a.K || m >= Ke) break;
+                float4 v;
+                if constexpr (RK > 0) v = hr[m + 1]; else v = hs[(m + 1) * 128 + threadIdx.x];
+                const float4 w = ws[m];
+                df_mac_lazy2(xrh[0], xih[0], xrl[0], xil[0], w.x, w.y, v.x, v.y);
+                df_mac_lazy2(xrh[1], xih[1], xrl[1], xil[1], w.x, w.y, v.z, v.w);
+            }
+            // Imaginary commutator weights i v: w h = -v h_i + i v h_r, summed
+            // as c += v h with paired FMAs (sr = -Im c, si = Re c: the same
+            // roundings as the scalar sums of the general branch).
+            float c0r = 0.f, c0i = 0.f, c1r = 0.f, c1i = 0.f;
+#pragma unroll
+            for (int m = 0; m < (RK > 0 ? RK : 1 << 30); ++m) {
+                if (m >= Ke) break;
+                if (m < a.K) continue;
+                float4 v;
+                if constexpr (RK > 0) v = hr[m + 1]; else v = hs[(m + 1) * 128 + threadIdx.x];
+                const float wz = ws[m].z;
+                fma2(c0r, c0i, wz, v.x, v.y);
+                fma2(c1r, c1i, wz, v.z, v.w);
+            }
+            sr[0] = -c0i;
+            si[0] = c0r;
+            sr[1] = -c1i;
+            si[1] = c1r;
+        } else
 #pragma unroll
         for (int m = 0; m < (RK > 0 ? RK : 1 << 30); ++m) {
             if (m >= Ke) break;
