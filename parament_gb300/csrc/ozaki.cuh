@@ -89,6 +89,9 @@ constexpr BLayout kBSlicesK = {(uint32_t)kBSlice, 0u, (uint32_t)kBlk, false};
 // the K-major blocks B_r^T = A_r and B_i^T = -A_i are the [A_r] and [-A_i]
 // blocks of A's slices, and A's row scales are B's column scales.
 constexpr BLayout kBFromHermA = {(uint32_t)kASlice, (uint32_t)kBlk, 0u, false};
+// The same B^T blocks as separate stacks, slice after slice: the [A_r]
+// blocks from sb on and the [-A_i] blocks from sb + h1 (stackable along N).
+__host__ __device__ constexpr BLayout herm_stacks(uint32_t h1) { return {(uint32_t)kBlk, 0u, h1, false}; }
 
 // Issues the MMAs of one sliced product (one thread).  Slices s < sa_n of A
 // at sa (kASlice bytes each) and t < sb_n of B at sb (laid out as bl says);
@@ -129,22 +132,30 @@ __device__ __forceinline__ void issue_product(uint32_t d_tmem, uint32_t sa, uint
     }
 }
 
-// The same product with MN-major B slices (kBSlice apart) stacked along N: for
-// A slice s, chains of MMAs with N = 64 n (n <= 4 B slices, N <= 256) cover
-// B slices t = 0 .. n_t - 1, n_t = min(sb_n, lmax - s + 1), and write levels
-// s + t at their tensor-memory columns d_tmem + 64 (s + t), which are
-// contiguous.  A is read once per chain instead of once per slice pair: the
-// N = 64 products are bound by the shared-memory operand reads (6 KB per
-// MMA).  With lmax < sb_n the chains of slice s = 0 cover every level; with
-// `fresh` they start them (first MMA of each without accumulate), otherwise
-// they add to what the levels hold.  Per level the sums are those of
-// issue_product, in the same order; other shapes go to issue_product.
+// Whether issue_product_stacked can stack the B slices of layout bl along N:
+// MN-major slices (one swizzle atom of N each, bl.stride apart: the leading
+// byte offset), or K-major slices whose 64-row blocks follow each other
+// (stride kBlk: the 8-row groups stay 1024 bytes apart across slices).
+__host__ __device__ constexpr bool stackable(BLayout bl) { return bl.mn || bl.stride == (uint32_t)kBlk; }
+
+// The same product with the B slices stacked along N: for A slice s, chains
+// of MMAs with N = 64 n (n <= 4 B slices, N <= 256) cover B slices
+// t = 0 .. n_t - 1, n_t = min(sb_n, lmax - s + 1), and write levels s + t at
+// their tensor-memory columns d_tmem + 64 (s + t), which are contiguous.  A is
+// read once per chain instead of once per slice pair: the N = 64 products are
+// bound by the shared-memory operand reads (6 KB per MMA).  With lmax < sb_n
+// the chains of slice s = 0 cover every level; with `fresh` they start them
+// (first MMA of each without accumulate), otherwise they add to what the
+// levels hold.  Per level the sums are those of issue_product, in the same
+// order; other shapes and layouts go to issue_product.
 __device__ __forceinline__ void issue_product_stacked(uint32_t d_tmem, uint32_t sa, uint32_t sb, int sa_n, int sb_n,
-                                                      int lmax, bool imag, bool fresh = true) {
-    if (lmax >= sb_n && fresh) {
-        issue_product(d_tmem, sa, sb, sa_n, sb_n, lmax, imag, kBSlicesMn);
+                                                      int lmax, bool imag, bool fresh = true,
+                                                      BLayout bl = kBSlicesMn) {
+    if ((lmax >= sb_n && fresh) || !stackable(bl)) {
+        issue_product(d_tmem, sa, sb, sa_n, sb_n, lmax, imag, bl);
         return;
     }
+    const uint32_t b_step = bl.mn ? 2048u : 32u;
     for (int s = 0; s < sa_n; ++s) {
         const int nt = min(sb_n, lmax - s + 1);
         const uint32_t a = sa + (uint32_t)s * kASlice;
@@ -152,18 +163,22 @@ __device__ __forceinline__ void issue_product_stacked(uint32_t d_tmem, uint32_t 
         const uint32_t a1 = imag ? a + kBlk : a;
         for (int t0 = 0; t0 < nt; t0 += 4) {
             const int n = min(4, nt - t0);
-            const uint32_t id_pos = idesc_bf16(false, true, 64 * n), id_neg = idesc_bf16(true, true, 64 * n);
+            const uint32_t id_pos = idesc_bf16(false, bl.mn, 64 * n), id_neg = idesc_bf16(true, bl.mn, 64 * n);
             const uint32_t d = d_tmem + 64u * (uint32_t)(s + t0);
-            const uint32_t b = sb + (uint32_t)t0 * kBSlice;
+            const uint32_t b = sb + (uint32_t)t0 * bl.stride;
             const uint32_t first = (s == 0 && fresh) ? 0u : 1u;
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk)
-                mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), desc_mn_sw128(b + 2048u * kk, (uint32_t)kBSlice), id_pos,
-                         kk > 0 ? 1u : first);
+            for (int kk = 0; kk < 4; ++kk) {
+                const uint32_t bb = b + bl.h0 + b_step * kk;
+                mma_bf16(d, tc::desc_k_sw128(a0 + 32u * kk), bl.mn ? desc_mn_sw128(bb, bl.stride) : tc::desc_k_sw128(bb),
+                         id_pos, kk > 0 ? 1u : first);
+            }
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk)
-                mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), desc_mn_sw128(b + kBlk + 2048u * kk, (uint32_t)kBSlice),
+            for (int kk = 0; kk < 4; ++kk) {
+                const uint32_t bb = b + bl.h1 + b_step * kk;
+                mma_bf16(d, tc::desc_k_sw128(a1 + 32u * kk), bl.mn ? desc_mn_sw128(bb, bl.stride) : tc::desc_k_sw128(bb),
                          imag ? id_neg : id_pos, 1u);
+            }
         }
     }
 }

@@ -82,6 +82,17 @@ constexpr size_t kTcdSB = (size_t)kTcdHi * oz::kBSlice;
 // for the odd part X Q and the B buffer is free for E^P while X Q runs.
 constexpr size_t kTcdSG = (size_t)kTcdG * oz::kASlice;
 constexpr size_t kTcdSmem = kTcdSA + kTcdSB + kTcdSG + 1024;
+// Hermitian steps also keep the B^T blocks of X (three slices) and of X^2
+// (two) as stacks that the tensor core reads along N: the [A_r] stack in the
+// tail of the A slice buffer (free while the polynomial runs), the [-A_i]
+// stack in the tail of the B slice buffer, past the lo planes of X (during
+// X^2) and past the A slices of X^4, X^6 (during those products).
+constexpr uint32_t kTcdStk0 = (uint32_t)kTcdX2 * oz::kASlice;  // in SA
+constexpr uint32_t kTcdStkX1 = 40960;                           // in SB
+constexpr uint32_t kTcdStkG1 = (uint32_t)kTcdG * oz::kASlice;   // in SB
+static_assert(kTcdStk0 + kTcdX2 * oz::kBlk <= kTcdSA, "[A_r] stack of X exceeds the A slice buffer");
+static_assert(kTcdStkX1 + kTcdX2 * oz::kBlk <= kTcdSB, "[-A_i] stack of X exceeds the B slice buffer");
+static_assert(kTcdStkG1 + kTcdG * oz::kBlk <= kTcdSB, "[-A_i] stack of X^2 exceeds the B slice buffer");
 // X_j reaches the lane layout through four planes (re hi, im hi, re lo, im
 // lo) of 64 rows padded to 68 floats (conflict-free 16-byte reads of a column
 // block by 32 consecutive rows).  k_split_assemble writes them for every step
@@ -95,6 +106,7 @@ constexpr int kTcdPlane = 64 * kTcdPlaneLd;
 constexpr uint32_t kTcdPairBytes = 2 * kTcdPlane * sizeof(float);
 static_assert(kTcdPairBytes <= kTcdSG && kTcdPairBytes <= kTcdSB && kTcdPairBytes % 16 == 0,
               "plane pairs exceed their slice buffers");
+static_assert(kTcdPairBytes <= kTcdStkX1, "the [-A_i] stack of X overlaps the lo planes");
 // Float index, within the planes of a step, of the flag that k_split_assemble
 // leaves in the row padding (plane 0, row 0, column 64): nonzero when X_j is
 // exactly Hermitian (Hermitian inputs, anti-Hermitian commutators, real
@@ -211,9 +223,13 @@ __device__ __forceinline__ float unscale_of(int mbits) {
 
 // With SETCOL the row scales also become the column scales (colmul): the
 // product's B is this A's conjugate transpose, read from the same slices.
-template <int S, bool DF, bool SETCOL = false>
+// With BSTACK the [A_r] and [-A_i] blocks are also written as two stacks,
+// slice after slice, at bt0 and bt1: the K-major B^T of a Hermitian operand
+// in the layout that stacks along N (ozaki.cuh, herm_stacks).
+template <int S, bool DF, bool SETCOL = false, bool BSTACK = false>
 __device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const TcdThread &t, int b,
-                                        const float (&hi)[16], const float (&lo)[16]) {
+                                        const float (&hi)[16], const float (&lo)[16], unsigned char *bt0 = nullptr,
+                                        unsigned char *bt1 = nullptr) {
     const int mb = sh.amax[b][t.r];
     if (t.p == 0 && t.cb == 0) {
         sh.rowmul[t.r] = unscale_of(mb);
@@ -234,7 +250,25 @@ __device__ __forceinline__ void store_a(TcdShared &sh, unsigned char *SA, const 
         } else {
             oz::peel8<S>(th, q);
         }
-        oz::store_a8<S>(SA, t.r, t.c0 + 8 * g, t.p, q);
+        if (BSTACK) {
+            const uint32_t off = oz::sw(t.r, t.c0 + 8 * g);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const uint4 v = oz::pack8(q[s]);
+                unsigned char *base = SA + s * oz::kASlice;
+                if (t.p == 0) {
+                    *reinterpret_cast<uint4 *>(base + oz::kBlk + off) = v;
+                    *reinterpret_cast<uint4 *>(bt0 + s * oz::kBlk + off) = v;
+                } else {
+                    const uint4 nv = oz::neg8(v);
+                    *reinterpret_cast<uint4 *>(base + 2 * oz::kBlk + off) = v;
+                    *reinterpret_cast<uint4 *>(base + off) = nv;
+                    *reinterpret_cast<uint4 *>(bt1 + s * oz::kBlk + off) = nv;
+                }
+            }
+        } else {
+            oz::store_a8<S>(SA, t.r, t.c0 + 8 * g, t.p, q);
+        }
     }
 }
 
@@ -283,10 +317,8 @@ __device__ __forceinline__ bool issue_sliced(TcdShared &sh, const TcdThread &t, 
     tc::fence_after_sync();
     if (!all_ok) return false;
     if (t.tid == 0) {
-        if (bl.mn)
-            oz::issue_product_stacked(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag);
-        else
-            oz::issue_product(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, bl);
+        oz::issue_product_stacked(sh.tmem_base, tc::smem_addr(SA), tc::smem_addr(SB), sa_n, sb_n, lmax, imag, true,
+                                  bl);
         tc::mma_commit(&sh.bar);
     }
     return true;
@@ -591,9 +623,11 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
         // ---- X^2
         if (herm) {
             reduce_max<true, false>(sh, t, nb, X, X);
-            store_a<kTcdX2, false, true>(sh, SA, t, nb, X, X);
+            store_a<kTcdX2, false, true, true>(sh, SA, t, nb, X, X, SA + kTcdStk0, SB + kTcdStkX1);
             nb ^= 1;
-            if (!issue_sliced(sh, t, SA, SA, kTcdX2, kTcdX2, kTcdX2 - 1, false, ok, oz::kBFromHermA)) break;
+            if (!issue_sliced(sh, t, SA, SA + kTcdStk0, kTcdX2, kTcdX2, kTcdX2 - 1, false, ok,
+                              oz::herm_stacks((uint32_t)kTcdSA - kTcdStk0 + kTcdStkX1)))
+                break;
             form_e();
             wait_sliced(sh, ncommit, ok);
         } else {
@@ -634,12 +668,12 @@ __global__ void __launch_bounds__(kTcdThreads, 1) k_split_tc(const __grid_consta
                 reduce_max<true, false>(sh, t, nb, G, G);
                 unsigned char *dst = k == 2 ? SG : SB;
                 if (k == 2)
-                    store_a<kTcdG, false, true>(sh, dst, t, nb, G, G);
+                    store_a<kTcdG, false, true, true>(sh, dst, t, nb, G, G, SA + kTcdStk0, SB + kTcdStkG1);
                 else
                     store_a<kTcdG, false>(sh, dst, t, nb, G, G);
                 nb ^= 1;
-                if (!(live = run_product(sh, t, dst, SG, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok,
-                                         oz::kBFromHermA)))
+                if (!(live = run_product(sh, t, dst, SA + kTcdStk0, kTcdG, kTcdG, kTcdG - 1, false, ncommit, ok,
+                                         oz::herm_stacks((uint32_t)kTcdSA - kTcdStk0 + kTcdStkG1))))
                     break;
             } else {
                 if (k == 2)
