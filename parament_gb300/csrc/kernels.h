@@ -44,6 +44,19 @@ int small_chunk_count(bool fp64, int d, int Ke, long long P, int num_sms);
 size_t small_smem_bytes(bool fp64, int d, int Ke);
 cudaError_t launch_small_steps(const StepLaunch &a);
 
+// The same plain complex64 propagation at d = 64 on the tcgen05 tensor cores
+// (small_tc.cu): per batch of up to 65536 steps, the X planes of the batch
+// (xplanes: small_tc_xplane_bytes(P)) and then one CTA per SM over the batch.
+// *nchunks receives the number of chunk products written (complex64), at most
+// small_tc_max_chunks(P, num_sms).  Non-null ev0 / ev1 are recorded around the
+// step-kernel launches; `fault` is the context's counter of bounded waits that
+// gave up.
+bool small_tc_applies(bool fp64, int d, int Ke, int M);
+size_t small_tc_xplane_bytes(long long P);
+int small_tc_max_chunks(long long P, int num_sms);
+cudaError_t launch_small_tc(const StepLaunch &l, int num_sms, float *xplanes, int *fault, int *nchunks,
+                            cudaEvent_t ev0, cudaEvent_t ev1);
+
 // C_b = alpha * A_b B_b + beta * Cin_b + diag * I for b < batch (all d x d,
 // row-major; strides in elements; beta = beta + i beta_im).  Cin may alias
 // Cout.  Cin may be null when beta == 0.

@@ -294,7 +294,38 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
                      c->fp64 ? h / 12.0 : (double)(float)h / 12.0};
     const double s = 2.0 / c->hnorm;
     cudaError_t e;
-    if (d <= kSmallMaxDim) {
+    if (small_tc_applies(c->fp64, d, (int)c->Ke, M)) {
+        // complex64 at d = 64: the same scheme with the products on the tensor
+        // cores (small_tc.cu); X planes per batch of steps, one complex64 chunk
+        // product per CTA, combined by the double-float tree.
+        const int nmax = small_tc_max_chunks(P, c->num_sms);
+        if (c->chunks.ensure(es * dd * nmax) != cudaSuccess || c->work.ensure(16 * dd * nmax) != cudaSuccess ||
+            c->X.ensure(16 * dd * ((nmax + 1) / 2)) != cudaSuccess ||
+            c->xplanes.ensure(small_tc_xplane_bytes(P)) != cudaSuccess)
+            return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+        StepLaunch l{};
+        l.fp64 = false;
+        l.d = d;
+        l.Ke = (int)c->Ke;
+        l.w = w;
+        l.M = M;
+        l.J = J.data();
+        l.s = s;
+        l.stack = c->stack.ptr;
+        l.carr = d_carr;
+        l.chunks = c->chunks.ptr;
+        l.P = P;
+        l.stream = stream;
+        int nch = 0;
+        e = launch_small_tc(l, c->num_sms, static_cast<float *>(c->xplanes.ptr), c->d_fault, &nch,
+                            c->timing ? c->ev_start : nullptr, c->timing ? c->ev_stop : nullptr);
+        int levels = 0;
+        if (e == cudaSuccess)
+            e = tree_df_c64(d, static_cast<const float2 *>(c->chunks.ptr), nch, c->work.ptr, c->X.ptr,
+                            static_cast<float2 *>(d_out), stream, &levels);
+        const long long batches = (P + 65535) / 65536;
+        c->launches = 2 * (int)batches + levels;
+    } else if (d <= kSmallMaxDim) {
         const int nch = small_chunk_count(c->fp64, d, (int)c->Ke, P, c->num_sms);
         // complex64: the chunk products are combined by the double-float tree
         // (complex128-sized buffers); complex128: by the FP64 tree.
@@ -421,9 +452,9 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
 
 // Whether an equiprop of this context may launch a kernel with bounded waits
 // (the tensor-core GEMM of complex64 contexts with d > 64, the tensor-core
-// split kernel).
+// split kernel, the tensor-core plain kernel at d = 64).
 static bool uses_tensor_kernels(const Ctx *c) {
-    return !c->fp64 && (c->dim > (unsigned)kSmallMaxDim || c->precision == PARAMENT_PRECISION_SPLIT);
+    return !c->fp64 && (c->dim >= (unsigned)kSmallMaxDim || c->precision == PARAMENT_PRECISION_SPLIT);
 }
 
 // Checks, order selection and dispatch shared by the host and device entry
