@@ -223,6 +223,12 @@ def split_slice_products(M):
     return 6 + 3 * max(0, q - 1) + 6 + 10
 
 
+# The step kernel each form of the d=64 workload runs.
+FORM_KERNELS = {"plain_c128": "k_small_steps<double> (FP64 pipe)",
+                "plain_c64": "k_small_tc (tcgen05, exact four-slice bf16 products; FP32 Clenshaw)",
+                "split_c64": "k_split_tc (tcgen05, exact bf16 slices; double-float E and running product)"}
+
+
 def run_form(torch, parament, w, form, K, W, flush, stream):
     precision = "fp64" if form == "plain_c128" else "fp32"
     ctx = parament.Parament(precision)
@@ -685,7 +691,8 @@ def run_ours(args, rank, world, local):
         ms = sum(r["ms"]) / len(r["ms"])
         summary[f] = {"steps_per_s": round(P / (ms * 1e-3), 1), "ms_per_prop": round(ms, 4),
                       "rel_err_vs_fp64": float(np.linalg.norm(r["U"] - Uo) / np.linalg.norm(Uo)),
-                      "M": r["M"], "kernel_ms": round(sum(r["kernel_ms"]) / len(r["kernel_ms"]), 4)}
+                      "M": r["M"], "kernel_ms": round(sum(r["kernel_ms"]) / len(r["kernel_ms"]), 4),
+                      "kernel": FORM_KERNELS.get(f)}
         if gpu128 is not None and f != "plain_c128":
             summary[f]["rel_err_vs_gpu_c128"] = float(np.linalg.norm(r["U"] - gpu128) / np.linalg.norm(gpu128))
         if f == "plain_c64" and Uo32 is not None:

@@ -65,27 +65,43 @@ struct SmallTcArgs {
 __device__ int g_small_tc_faults;
 
 // X planes of steps s_off .. s_off + n - 1.  Thread f of CTA row blockIdx.x
-// owns float4 f of every expansion matrix (complex elements 2f, 2f + 1); the
-// CTA forms the complex64 weights of its kAsmSteps steps in shared memory and
-// walks them.  X = H_0 + sum_m w_m H_m by complex fused multiply-adds in slot
-// order, as in k_small_steps.
+// owns float4 f of every expansion matrix (complex elements 2f, 2f + 1) and
+// keeps that slice of the stack in registers (RK > 0: up to RK + 1 matrices,
+// loops unrolled) or in shared memory (RK = 0); the CTA forms the complex64
+// weights of its kPlainAsmSteps steps in shared memory and walks them.
+// X = H_0 + sum_m w_m H_m by complex fused multiply-adds in slot order, as in
+// k_small_steps.
 constexpr int kPlainAsmSteps = 32;
+constexpr int kPlainAsmRegKe = 15;  // largest Ke with the stack slice in registers
+template <int RK>
 __global__ void __launch_bounds__(128) k_plain_assemble(const float2 *__restrict__ stack, const float2 *__restrict__ carr,
                                                         WeightSpec w, int Ke, float *xp, long long s_off,
                                                         long long n) {
+    extern __shared__ float4 hs[];  // RK = 0: (1 + Ke) x 128 float4 of the stack
     __shared__ float2 ws[kPlainAsmSteps * kStcMaxKe];
     const int f = blockIdx.x * 128 + threadIdx.x;
     const long long sb = (long long)blockIdx.y * kPlainAsmSteps;
     const int ns = (int)(n - sb < kPlainAsmSteps ? n - sb : kPlainAsmSteps);
+    const float4 *stack4 = reinterpret_cast<const float4 *>(stack);
+    float4 hr[RK + 1];
+    if constexpr (RK > 0) {
+#pragma unroll
+        for (int m = 0; m <= RK; ++m) hr[m] = m <= Ke ? stack4[(size_t)m * 2048 + f] : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        for (int m = 0; m <= Ke; ++m) hs[m * 128 + threadIdx.x] = stack4[(size_t)m * 2048 + f];
+    }
     for (int i = threadIdx.x; i < ns * Ke; i += 128) ws[i] = step_weight(carr, w, i % Ke, s_off + sb + i / Ke);
     __syncthreads();
-    const float4 *stack4 = reinterpret_cast<const float4 *>(stack);
     const int row = f >> 5, col = 2 * (f & 31);
     for (int k = 0; k < ns; ++k) {
-        const float4 h0 = stack4[f];
+        float4 h0;
+        if constexpr (RK > 0) h0 = hr[0]; else h0 = hs[threadIdx.x];
         float2 v0 = make_float2(h0.x, h0.y), v1 = make_float2(h0.z, h0.w);
-        for (int m = 0; m < Ke; ++m) {
-            const float4 h = stack4[(size_t)(m + 1) * 2048 + f];
+#pragma unroll
+        for (int m = 0; m < (RK > 0 ? RK : 1 << 30); ++m) {
+            if (m >= Ke) break;
+            float4 h;
+            if constexpr (RK > 0) h = hr[m + 1]; else h = hs[(m + 1) * 128 + threadIdx.x];
             const float2 wm = ws[k * Ke + m];
             cfma(v0, wm, make_float2(h.x, h.y));
             cfma(v1, wm, make_float2(h.z, h.w));
@@ -296,12 +312,22 @@ cudaError_t launch_small_tc(const StepLaunch &l, int num_sms, float *xplanes, in
     const WeightSpec w{l.w.pts, l.w.K, l.w.amps, l.w.mode, l.w.magnus, l.w.hfac};
     const float2 *stack = static_cast<const float2 *>(l.stack);
     const float2 *carr = static_cast<const float2 *>(l.carr);
+    const bool asm_reg = l.Ke <= kPlainAsmRegKe;
+    const void *asm_fn = asm_reg ? reinterpret_cast<const void *>(&k_plain_assemble<kPlainAsmRegKe>)
+                                 : reinterpret_cast<const void *>(&k_plain_assemble<0>);
+    const size_t hs_bytes = asm_reg ? 0 : sizeof(float4) * 128 * (size_t)(l.Ke + 1);
+    if ((e = cudaFuncSetAttribute(asm_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hs_bytes)) != cudaSuccess)
+        return e;
     int total = 0;
     for (long long b0 = 0; b0 < l.P; b0 += kSmallXBatch) {
         const long long nb = std::min<long long>(kSmallXBatch, l.P - b0);
         const dim3 ag(16, (unsigned)((nb + kPlainAsmSteps - 1) / kPlainAsmSteps));
-        k_plain_assemble<<<ag, 128, 0, l.stream>>>(stack, carr, w, l.Ke, xplanes, b0, nb);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        int ke = l.Ke;
+        long long off = b0, cnt = nb;
+        float *xpp = xplanes;
+        WeightSpec wv = w;
+        void *args[] = {const_cast<float2 **>(&stack), const_cast<float2 **>(&carr), &wv, &ke, &xpp, &off, &cnt};
+        if ((e = cudaLaunchKernel(asm_fn, ag, dim3(128), args, hs_bytes, l.stream)) != cudaSuccess) return e;
         a.P = nb;
         a.nchunks = (int)std::max<long long>(1, std::min<long long>((long long)num_sms, nb));
         a.chunks = static_cast<float2 *>(l.chunks) + (size_t)total * 4096;
