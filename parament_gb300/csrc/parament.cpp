@@ -294,15 +294,15 @@ static Parament_ErrorCode run_plain(Ctx *c, const void *d_carr, unsigned pts, un
                      c->fp64 ? h / 12.0 : (double)(float)h / 12.0};
     const double s = 2.0 / c->hnorm;
     cudaError_t e;
-    if (small_tc_applies(c->fp64, d, (int)c->Ke, M)) {
-        // complex64 at d = 64: the same scheme with the products on the tensor
-        // cores (small_tc.cu); X planes per batch of steps, one complex64 chunk
-        // product per CTA, combined by the double-float tree.
-        const int nmax = small_tc_max_chunks(P, c->num_sms);
-        if (c->chunks.ensure(es * dd * nmax) != cudaSuccess || c->work.ensure(16 * dd * nmax) != cudaSuccess ||
-            c->X.ensure(16 * dd * ((nmax + 1) / 2)) != cudaSuccess ||
-            c->xplanes.ensure(small_tc_xplane_bytes(P)) != cudaSuccess)
-            return PARAMENT_STATUS_DEVICE_ALLOC_FAILED;
+    // complex64 at d = 64: the same scheme with the products on the tensor
+    // cores (small_tc.cu); X planes per batch of steps, one complex64 chunk
+    // product per CTA, combined by the double-float tree.  Where the planes
+    // (up to 2.3 GB) cannot be allocated, the FP32 SIMT kernel below runs,
+    // which needs only the chunk buffers.
+    const int nmax = small_tc_max_chunks(P, c->num_sms);
+    if (small_tc_applies(c->fp64, d, (int)c->Ke, M) && c->chunks.ensure(es * dd * nmax) == cudaSuccess &&
+        c->work.ensure(16 * dd * nmax) == cudaSuccess && c->X.ensure(16 * dd * ((nmax + 1) / 2)) == cudaSuccess &&
+        c->xplanes.ensure(small_tc_xplane_bytes(P)) == cudaSuccess) {
         StepLaunch l{};
         l.fp64 = false;
         l.d = d;

@@ -6,7 +6,8 @@ complex64 parity bar of 1e-5 relative Frobenius error, and against the FP32
 SIMT kernel it replaces (tensor cores switched off through
 PARAMENT_DISABLE_TENSOR_CORES in a child process).  Cases: every quadrature
 mode with Magnus, complex samples, fewer steps than SMs, manual Chebyshev
-orders from 1 to 15, and more steps than one batch of X planes.
+orders from 1 to 15, more steps than one batch of X planes, and the fall-back
+to the SIMT kernel when the plane buffer cannot be allocated.
 """
 import os
 import subprocess
@@ -113,3 +114,44 @@ def test_matches_simt_kernel(built_lib):
             outs.append(np.load(f).astype(np.complex128))
     assert relerr(outs[0], outs[1]) < TOL
     assert not np.array_equal(outs[0], outs[1])  # two different kernels ran
+
+
+_FALLBACK_CASE = """
+import sys, numpy as np, torch
+import parament_gb300 as p
+from parament_gb300.workloads import hermitian
+rng = np.random.default_rng(91)
+c = lambda x: x.astype(np.complex64)
+H0 = hermitian(rng, 64, 5.0)
+H1 = np.stack([hermitian(rng, 64, 1.0) for _ in range(2)])
+carr = rng.standard_normal((2, 20000))
+ctx = p.Parament('fp32')
+ctx.set_hamiltonian(c(H0), *c(H1))
+U = ctx.equiprop_device(1e-3, torch.tensor(c(carr), device='cuda'))
+torch.cuda.synchronize()
+np.save(sys.argv[1], U.cpu().numpy())
+print('BYTES', ctx.device_memory_bytes())
+"""
+
+
+def test_falls_back_when_planes_cannot_be_allocated(built_lib):
+    """Host-side fault injection fails the X plane buffer (the fifth device
+    allocation: stack, chunks, work, tree buffer, planes): the propagation runs
+    on the FP32 SIMT kernel, which holds no planes, and still meets the bar."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with tempfile.TemporaryDirectory() as tmp:
+        f = os.path.join(tmp, "U.npy")
+        env = dict(os.environ, PARAMENT_FAIL_ALLOC_AFTER="4")
+        r = subprocess.run([sys.executable, "-c", _FALLBACK_CASE, f], cwd=root, env=env, capture_output=True,
+                           text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        U = np.load(f).astype(np.complex128)
+    held = int(r.stdout.split("BYTES")[1].split()[0])
+    assert held < 200 << 20, held  # no plane buffer (it would take 696 MB)
+    from parament_gb300.workloads import hermitian
+    rng = np.random.default_rng(91)
+    H0 = c64(hermitian(rng, 64, 5.0))
+    H1 = c64(np.stack([hermitian(rng, 64, 1.0) for _ in range(2)]))
+    carr = c64(rng.standard_normal((2, 20000)))
+    Uo = oracle.equiprop(H0, H1, carr, 1e-3, single=True, nthreads=os.cpu_count())[0]
+    assert relerr(U, Uo) < TOL
