@@ -130,7 +130,7 @@ ctx.set_hamiltonian(c(H0), *c(H1))
 U = ctx.equiprop_device(1e-3, torch.tensor(c(carr), device='cuda'))
 torch.cuda.synchronize()
 np.save(sys.argv[1], U.cpu().numpy())
-print('BYTES', ctx.device_memory_bytes())
+print('BYTES', ctx.device_memory_bytes)
 """
 
 
