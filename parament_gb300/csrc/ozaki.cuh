@@ -85,12 +85,11 @@ struct BLayout {
 // B slices of their own: [B_r][B_i] blocks per slice, MN-major or K-major.
 constexpr BLayout kBSlicesMn = {(uint32_t)kBSlice, 0u, (uint32_t)kBlk, true};
 constexpr BLayout kBSlicesK = {(uint32_t)kBSlice, 0u, (uint32_t)kBlk, false};
-// B = A^H read from the A slices of a Hermitian operand: B^T = conj(A), so
-// the K-major blocks B_r^T = A_r and B_i^T = -A_i are the [A_r] and [-A_i]
-// blocks of A's slices, and A's row scales are B's column scales.
-constexpr BLayout kBFromHermA = {(uint32_t)kASlice, (uint32_t)kBlk, 0u, false};
-// The same B^T blocks as separate stacks, slice after slice: the [A_r]
-// blocks from sb on and the [-A_i] blocks from sb + h1 (stackable along N).
+// B = A^H for a Hermitian operand A: B^T = conj(A), so the K-major blocks
+// B_r^T = A_r and B_i^T = -A_i are copies of A's [A_r] and [-A_i] blocks, and
+// A's row scales are B's column scales.  The copies are written as two
+// stacks, slice after slice: the [A_r] blocks from sb on and the [-A_i]
+// blocks from sb + h1 (stackable along N).
 __host__ __device__ constexpr BLayout herm_stacks(uint32_t h1) { return {(uint32_t)kBlk, 0u, h1, false}; }
 
 // Issues the MMAs of one sliced product (one thread).  Slices s < sa_n of A

@@ -33,12 +33,13 @@
 // When X_j is exactly Hermitian (Hermitian inputs and real control samples;
 // k_split_assemble flags each step), so is the computed X^2 (exact integer
 // level sums, symmetric scales), and the products X X, X^2 X^2 and
-// X^(2k-2) X^2 take their B operand straight from the A slices of X or X^2:
-// B^T = conj(A), the [A_r] and [-A_i] blocks (ozaki.cuh, kBFromHermA), with
-// the row scales as column scales.  The slices are the same numbers the B
-// slicing would produce, so the result is bit-identical; such a step just
-// skips the B slicing of X and X^2 with their column maxima, and forms E from
-// the planes while the tensor core runs X^2.
+// X^(2k-2) X^2 take their B operand from the A slices of X or X^2:
+// B^T = conj(A), copies of the [A_r] and [-A_i] blocks written as stacks
+// along N while A is sliced (ozaki.cuh, herm_stacks), with the row scales as
+// column scales.  The slices are the same numbers the B slicing would
+// produce, so the result is bit-identical; such a step just skips the B
+// slicing of X and X^2 with their column maxima, and forms E from the planes
+// while the tensor core runs X^2.
 //
 // Layout of one CTA (512 threads, one per SM): shared memory holds the A
 // slices (4 x 24 KB), the B slices (4 x 16 KB) and a third buffer (2 x 24 KB)
