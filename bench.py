@@ -263,8 +263,11 @@ def run_form(torch, parament, w, form, K, W, flush, stream):
     launches = int(getattr(lib, "Parament_lastLaunchCount" + sfx)(ctx._handle))
     # End to end through the reference-facing C-ABI with host buffers, after one
     # untimed call (the first host call grows the context's sample buffers).
+    # The host samples are one (K, pts) array in the context's precision, as
+    # a caller of that precision holds them; the wrapper passes such rows on
+    # without a copy.
     e2e = []
-    host_carr = [np.ascontiguousarray(r) for r in w["carr"]]
+    host_carr = np.ascontiguousarray(w["carr"], dtype=np.complex128 if precision == "fp64" else np.complex64)
     ctx.equiprop(w["dt"], *host_carr)
     for _ in range(max(2, K)):
         flush.zero_()  # L2 flush between timed calls, outside the timed region
@@ -520,7 +523,7 @@ def plain_d16_block(torch, parament, K_steps, W_steps, flush, stream, lib_peaks)
     launches = int(lib.Parament_lastLaunchCount_fp64(ctx._handle))
     M = ctx.last_iteration_cycles
     U = out.cpu().numpy()
-    host = [np.ascontiguousarray(r) for r in w["carr"]]
+    host = np.ascontiguousarray(w["carr"], dtype=np.complex128)
     ctx.equiprop(w["dt"], *host)
     e2e = []
     for _ in range(max(K_steps, 20)):

@@ -52,6 +52,26 @@ _EXCEPTIONS = {
 _CUDA_STREAM_LEGACY = 1
 
 
+def _pack_samples(carr, ctype, amps, pts):
+    """The control samples as one C-contiguous (amps * pts) array of ``ctype``.
+
+    When the rows are consecutive rows of one C-contiguous 2-D array of that
+    type (``equiprop(dt, *samples)`` with ``samples`` of shape (amps, pts)),
+    that array is passed on as it is; otherwise the rows are copied (and
+    converted) into a new one, as the reference's wrapper does.
+    """
+    if amps and all(isinstance(c, np.ndarray) for c in carr):
+        base = carr[0].base
+        if (isinstance(base, np.ndarray) and base.dtype == ctype and base.ndim == 2 and base.shape == (amps, pts)
+                and base.flags.c_contiguous):
+            start = base.__array_interface__['data'][0]
+            step = pts * base.itemsize
+            if all(c.base is base and c.__array_interface__['data'][0] == start + k * step
+                   for k, c in enumerate(carr)):
+                return base.reshape(-1)
+    return np.ascontiguousarray(np.ravel(np.asarray(carr, dtype=ctype).reshape(amps, pts), order='C'))
+
+
 def _stream_handle(stream):
     return ctypes.c_void_p(stream.cuda_stream or _CUDA_STREAM_LEGACY)
 
@@ -186,7 +206,7 @@ class Parament:
         if any(np.shape(c) != (pts,) for c in carr):
             raise ValueError("All amplitude arrays must have the same length.")
         output = np.zeros(self.dim ** 2, dtype=self._ctype)
-        samples = np.ascontiguousarray(np.ravel(np.asarray(carr, dtype=self._ctype).reshape(amps, pts), order='C'))
+        samples = _pack_samples(carr, self._ctype, amps, pts)
         if samples.size == 0:
             samples = np.zeros(1, dtype=self._ctype)
         self._check_error(self._fn('Parament_equiprop')(self._handle, samples, float(dt), pts, amps, output))

@@ -79,3 +79,22 @@ def test_wrapper_rejects_bad_precision(built_lib):
     import parament_gb300 as parament
     with pytest.raises(ValueError, match="precision must be either"):
         parament.Parament("fp16")
+
+
+def test_sample_packing_passes_contiguous_rows_through():
+    """equiprop's sample packing: rows of one C-contiguous array of the
+    context's type go through without a copy; anything else is copied and
+    converted, with the same values."""
+    from parament_gb300.parament import _pack_samples
+    rng = np.random.default_rng(3)
+    base = np.ascontiguousarray((rng.standard_normal((3, 50)) + 1j * rng.standard_normal((3, 50))).astype(np.complex64))
+    packed = _pack_samples(tuple(base), np.complex64, 3, 50)
+    assert np.shares_memory(packed, base) and np.array_equal(packed, base.ravel())
+    # another type, a subset of rows, reordered rows, separate arrays: copies
+    for carr in (tuple(base[:2]), (base[1], base[0], base[2]), tuple(np.array(r) for r in base)):
+        for ctype in (np.complex64, np.complex128):
+            out = _pack_samples(carr, ctype, len(carr), 50)
+            assert out.dtype == ctype and out.flags.c_contiguous and not np.shares_memory(out, base)
+            assert np.array_equal(out, np.concatenate([np.asarray(c, ctype) for c in carr]))
+    out = _pack_samples(tuple(base), np.complex128, 3, 50)
+    assert not np.shares_memory(out, base) and np.array_equal(out, base.ravel().astype(np.complex128))
